@@ -1,0 +1,224 @@
+/*
+ * isosim.h -- C ABI of the GB300 isosurface-similarity engine.
+ *
+ * Plain C types only (no CUDA, C++ or torch types).  Every entry point that can
+ * fail returns an int status (ISO_OK == 0, negative on error) and never exits
+ * the process; iso_last_error() returns the message of the calling thread's
+ * most recent failure.  The reference instead terminates through
+ * checkCudaErrors (isosurfaces_cuda/hdr/helper_cuda.h:968-996).
+ *
+ * Volumes are float32 in the reference's flattened "img" order (z fastest,
+ * img[x*Y*Z + y*Z + z]; types/src/Isosurface.cpp:185-200).  Pointer arguments
+ * documented as "host or device" are read with cudaMemcpyDefault, so both
+ * pageable/pinned host memory and device memory are accepted.
+ *
+ * Paths in citations are relative to the reference's isosurfaces_lib/ folder.
+ */
+#ifndef ISOSIM_H
+#define ISOSIM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* C99 _Bool and C++ bool share size and ABI */
+#ifdef __cplusplus
+#define ISO_BOOL bool
+#else
+#define ISO_BOOL _Bool
+#endif
+
+#if defined(__GNUC__)
+#define ISO_API __attribute__((visibility("default")))
+#else
+#define ISO_API
+#endif
+
+/* status codes */
+#define ISO_OK 0
+#define ISO_ERR_ARG (-1)      /* invalid argument */
+#define ISO_ERR_CUDA (-2)     /* CUDA runtime error */
+#define ISO_ERR_CAPACITY (-3) /* caller buffer or fixed-size structure too small */
+#define ISO_ERR_NOMEM (-4)    /* device or host allocation failed */
+#define ISO_ERR_INTERNAL (-5) /* a device-side consistency check failed */
+
+/* surface extraction */
+#define ISO_SURFACE_MC 0     /* marching cubes: cudaMarchingCube (isosurfaces_cuda/src/MarchingCube.cpp:588) */
+#define ISO_SURFACE_APPROX 1 /* voxel approximation: approximate_isosurfaces_h (IsosurfaceApproximation.cu:160) */
+
+/* marching-cubes coordinate frame */
+#define ISO_FRAME_REF 0   /* the reference kernel's frame: the z-fastest volume indexed x-fastest (MarchingCube.cu:60-65) */
+#define ISO_FRAME_CANON 1 /* geometric frame of the volume (x slowest, z fastest) */
+
+/* distance-field method; all give bit-identical fields */
+#define ISO_DF_BRUTE 0 /* every sample against every surface point, FP32 */
+#define ISO_DF_LBVH 1  /* linear BVH (Morton codes, radix sort, Karras hierarchy, stack query) */
+
+/* marching-cubes result flags (iso_surface_stats.flags) */
+#define ISO_MC_REF_DROPPED 1 /* more than V-3 triangle vertices: the reference drops triangles here */
+
+typedef struct iso_ctx iso_ctx;
+
+typedef struct iso_opts {
+    int surface;      /* ISO_SURFACE_* */
+    int frame;        /* ISO_FRAME_* (marching cubes only) */
+    int df_method;    /* ISO_DF_* */
+    int df_downscale; /* >= 1; DF grid is (X/ds, Y/ds, Z/ds) */
+    int bins;         /* joint-histogram bins per axis, 2..256 */
+} iso_opts;
+
+typedef struct iso_surface_stats {
+    int64_t points;        /* unique surface points (0 = empty surface) */
+    int64_t active_voxels; /* cells with a non-empty case (marching cubes) */
+    int64_t total_verts;   /* sum of per-case triangle-vertex counts (marching cubes) */
+    int32_t flags;         /* ISO_MC_* */
+    int32_t reserved;
+} iso_surface_stats;
+
+typedef struct iso_rep {
+    float isovalue; /* as the reference leaves it: the isovalue of the previously popped pick */
+    float priority;
+    int32_t id;     /* isovalue index */
+    int32_t map_id; /* row of the similarity map */
+} iso_rep;
+
+typedef struct iso_timing {
+    float surface_ms, distance_ms, histogram_ms, total_ms;
+} iso_timing;
+
+/* ---------------------------------------------------------------------- */
+/* Context                                                                 */
+/* ---------------------------------------------------------------------- */
+
+/* Creates a context on `device` with its own CUDA stream and a grow-only
+ * device arena reused by every call.  One context per host thread. */
+ISO_API int iso_ctx_create(int device, iso_ctx **out);
+ISO_API void iso_ctx_destroy(iso_ctx *ctx);
+/* The context's cudaStream_t, as void*. */
+ISO_API void *iso_ctx_stream(iso_ctx *ctx);
+/* Bytes currently held by the context's device arena. */
+ISO_API size_t iso_ctx_device_bytes(iso_ctx *ctx);
+/* Thread-local message of the last failure ("" if none). */
+ISO_API const char *iso_last_error(void);
+/* Number of kernel launches issued by this context so far. */
+ISO_API int64_t iso_ctx_launches(iso_ctx *ctx);
+
+/* ---------------------------------------------------------------------- */
+/* Whole-volume pipeline (replaces the per-isovalue loop of Single::run,   */
+/* runtime/src/Single.cpp:193-243, and calculate_histogram_W,              */
+/* isosurfaces_cuda/funcs.cpp:148-205)                                     */
+/* ---------------------------------------------------------------------- */
+
+/* volume: X*Y*Z floats (host or device).  isovalues: n floats (host).
+ * Surfaces for all isovalues, distance fields of the non-empty ones, all-pairs
+ * joint histograms and FP64 normalised mutual information.  Outputs (host or
+ * device): ism_out m*m floats row-major, field_ids_out the isovalue index of
+ * each row (n capacity), *m_out = number of non-empty surfaces.  stats_out
+ * (n entries) and timing_out may be NULL. */
+ISO_API int iso_ism(iso_ctx *ctx, const float *volume, int X, int Y, int Z,
+                    const float *isovalues, int n, const iso_opts *opts,
+                    float *ism_out, int32_t *field_ids_out, int32_t *m_out,
+                    iso_surface_stats *stats_out, iso_timing *timing_out);
+
+/* Cross map between two field sets of equal size m (the multi mode of
+ * calculate_histogram_h, isosurfaces_cuda/src/JointHistogram.cu:309-318,
+ * used by MultiVar::computeMultiMap, runtime/src/MultiVar.cpp:170-249):
+ * out[i*m + j] = NMI(fields_a[i], fields_b[j]).  fields_*: m*n floats. */
+ISO_API int iso_cross_map(iso_ctx *ctx, const float *fields_a, const float *fields_b, int m, int64_t n,
+                          int bins, float *out);
+
+/* ---------------------------------------------------------------------- */
+/* Stage entry points                                                      */
+/* ---------------------------------------------------------------------- */
+
+/* Surface points of n isovalues.  counts_out[k] = unique points of isovalue k.
+ * points_out (host or device, may be NULL to query counts): concatenated xyz
+ * float triples in isovalue order, marching cubes vertices sorted
+ * lexicographically per isovalue (the reference's sort + unique order),
+ * approximation cells as float-converted integer triples in linear cell order.
+ * Returns ISO_ERR_CAPACITY if cap_points < sum(counts). */
+ISO_API int iso_surface_points(iso_ctx *ctx, const float *volume, int X, int Y, int Z,
+                               const float *isovalues, int n, int surface, int frame,
+                               int64_t *counts_out, float *points_out, int64_t cap_points,
+                               iso_surface_stats *stats_out);
+
+/* Distance field of one point set given in normalised coordinates (p / max(X,Y,Z),
+ * isosurfaces_cuda/funcs.cpp:209-233): out[i] = sqrt(min_p |s_i - p|^2) over the
+ * sample grid of isosurfaces_cuda/src/BVH.cu:393-406 (a single point gives the
+ * squared distance, BVH.cu:604-611).  points: P xyz triples (host or device);
+ * out: (X/ds)(Y/ds)(Z/ds) floats (host or device). */
+ISO_API int iso_distance_field(iso_ctx *ctx, const float *points, int64_t P, int X, int Y, int Z,
+                               int downscale, int method, float *out);
+
+/* Similarity map of m fields of n values each (fields: m*n, host or device):
+ * ism_out m*m (FP64 MI rounded to float).  joint_out (may be NULL): m*m*bins*bins
+ * uint32 histograms of every ordered pair (row = bucket of field i). */
+ISO_API int iso_similarity_map(iso_ctx *ctx, const float *fields, int m, int64_t n, int bins,
+                               float *ism_out, uint32_t *joint_out);
+
+/* Representative isovalues (types/src/SimilarityMap.cpp:88-227): Bruckner's
+ * recursive prioritisation + greedy re-weighted selection; ties go to the lower
+ * map index.  ism: m*m host floats; ids: isovalue index per row; isovalues:
+ * indexed by id.  Writes min(cnt, m) entries, returns that count (or < 0). */
+ISO_API int iso_select_representatives(const float *ism, int m, const int32_t *ids, const float *isovalues,
+                                       int cnt, iso_rep *out);
+
+/* Isovalues of runtime/src/Single.cpp:286-392: uniform != 0 equalises a
+ * 65536-bin histogram of the volume (computed on the GPU) into n groups, else
+ * min + i*(max-min)/n.  vmin/vmax: the volume's real range
+ * (types/src/Isosurface.cpp:48-75, see iso_real_range). */
+ISO_API int iso_isovalues(iso_ctx *ctx, const float *volume, int64_t V, float vmin, float vmax, int n,
+                          int uniform, float *out);
+
+/* Real min/max of values within [cfg_min, cfg_max] (types/src/Isosurface.cpp:48-75). */
+ISO_API int iso_real_range(iso_ctx *ctx, const float *volume, int64_t V, float cfg_min, float cfg_max,
+                           float *out_min, float *out_max);
+
+/* ---------------------------------------------------------------------- */
+/* Reference-named entry points (drop-in for isosurfaces_cuda/funcs.h)     */
+/* ---------------------------------------------------------------------- */
+
+typedef struct iso_int3 { int32_t x, y, z; } iso_int3;
+
+/* isosurfaces_cuda/funcs.h:32-36, JointHistogram.cu:266-420.  Same arguments
+ * and meaning: numFields fields (2*numFields with multi), similarity map
+ * h_simMap (simMapSize x simMapSize), per-ordered-pair column and row sums
+ * (numFields^2 * histogramSize each).  h_jointHist is left untouched, as the
+ * reference leaves it (its copy-back is commented out, :397).  MI is FP64.
+ * Uses a process-wide context on device 0. */
+ISO_API void calculate_histogram_h(float **distanceFields, float *minValues, float *maxValues, const int fieldSize,
+                                   const unsigned long numFields, const unsigned long histogramSize,
+                                   unsigned int *h_jointHist, unsigned int *h_colSums, unsigned int *h_rowSums,
+                                   float *h_simMap, const int simMapSize, const ISO_BOOL multi);
+
+/* isosurfaces_cuda/funcs.h:23-24, IsosurfaceApproximation.cu:159-212: cells
+ * crossing the isovalue as int triples in linear order; *h_points is
+ * malloc'd by the callee and freed by the caller with free().  scale must be 1
+ * (the only value the reference's callers use, types/src/Isosurface.cpp:284).
+ * Returns the count, or a negative status. */
+ISO_API long approximate_isosurfaces_h(float *h_data, float isovalue, const int dimX, const int dimY, const int dimZ,
+                                       const int scale, iso_int3 **h_points);
+
+/* C form of cudaMarchingCube (isosurfaces_cuda/hdr/MarchingCube.h:11-16,
+ * MarchingCube.cpp:588-710): unique vertices (x,y,z,w=1) sorted
+ * lexicographically, *out_xyzw malloc'd by the callee.  maxVerts as in the
+ * reference (triangles whose first index is >= maxVerts-3 are dropped there;
+ * here ISO_ERR_CAPACITY is returned in that case).  Reference frame. */
+ISO_API int iso_marching_cube_h(float iso, int dimX, int dimY, int dimZ, const float *h_volume, int maxVerts,
+                                float **out_xyzw, long *out_count);
+
+/* C form of generateHierarchy_h (isosurfaces_cuda/funcs.h:43-44, BVH.cu:814-875)
+ * for the non-sampleGiven case: points already normalised, distances written to
+ * h_distances ((X/ds)(Y/ds)(Z/ds) floats).  numSamples (the reference's 1500
+ * pre-sampled upper bound) does not change the result and is accepted for
+ * signature parity. */
+ISO_API int iso_generate_hierarchy_h(const float *points_xyz, long numPoints, int dimX, int dimY, int dimZ,
+                                     float *h_distances, int numSamples, int dfDownscale);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

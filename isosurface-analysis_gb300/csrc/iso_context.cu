@@ -1,0 +1,137 @@
+// iso_context.cu -- contexts, the device arena and error reporting.
+#include <cstdarg>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include "iso_internal.cuh"
+
+static thread_local char g_last_error[1024] = "";
+
+int iso_fail(int code, const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof g_last_error, fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+void iso_clear_error() { g_last_error[0] = '\0'; }
+
+extern "C" const char *iso_last_error(void) { return g_last_error; }
+
+extern "C" int iso_ctx_create(int device, iso_ctx **out)
+{
+    if (!out) return iso_fail(ISO_ERR_ARG, "iso_ctx_create: out is NULL");
+    *out = nullptr;
+    int count = 0;
+    ISO_CUDA(cudaGetDeviceCount(&count));
+    if (device < 0 || device >= count)
+        return iso_fail(ISO_ERR_ARG, "iso_ctx_create: device %d out of range (%d devices)", device, count);
+    ISO_CUDA(cudaSetDevice(device));
+    iso_ctx *ctx = new iso_ctx();
+    ctx->device = device;
+    cudaError_t e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return iso_fail(ISO_ERR_CUDA, "iso_ctx_create: %s", cudaGetErrorString(e));
+    }
+    *out = ctx;
+    return ISO_OK;
+}
+
+extern "C" void iso_ctx_destroy(iso_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (int b = 0; b < BUF_COUNT_; ++b)
+        if (ctx->buf[b]) cudaFree(ctx->buf[b]);
+    if (ctx->host_pinned) cudaFreeHost(ctx->host_pinned);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+extern "C" void *iso_ctx_stream(iso_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+extern "C" int64_t iso_ctx_launches(iso_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+extern "C" size_t iso_ctx_device_bytes(iso_ctx *ctx)
+{
+    size_t s = 0;
+    if (ctx)
+        for (int b = 0; b < BUF_COUNT_; ++b) s += ctx->cap[b];
+    return s;
+}
+
+int iso_buf(iso_ctx *ctx, IsoBuf b, size_t bytes, void **out)
+{
+    if (bytes == 0) bytes = 256;
+    if (ctx->cap[b] < bytes) {
+        if (ctx->buf[b]) {
+            // the old buffer may still be read by queued work on this stream
+            ISO_CUDA(cudaStreamSynchronize(ctx->stream));
+            ISO_CUDA(cudaFree(ctx->buf[b]));
+            ctx->buf[b] = nullptr;
+            ctx->cap[b] = 0;
+        }
+        size_t want = bytes + bytes / 8;
+        want = (want + 4095) & ~size_t(4095);
+        void *p = nullptr;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return iso_fail(ISO_ERR_NOMEM, "device allocation of %zu bytes failed: %s", want, cudaGetErrorString(e));
+        }
+        ctx->buf[b] = p;
+        ctx->cap[b] = want;
+    }
+    *out = ctx->buf[b];
+    return ISO_OK;
+}
+
+int iso_host_scratch(iso_ctx *ctx, size_t bytes, void **out)
+{
+    if (ctx->host_pinned_cap < bytes) {
+        if (ctx->host_pinned) {
+            ISO_CUDA(cudaStreamSynchronize(ctx->stream));
+            cudaFreeHost(ctx->host_pinned);
+            ctx->host_pinned = nullptr;
+            ctx->host_pinned_cap = 0;
+        }
+        size_t want = (bytes + bytes / 4 + 4095) & ~size_t(4095);
+        void *p = nullptr;
+        if (cudaMallocHost(&p, want) != cudaSuccess) {
+            cudaGetLastError();
+            return iso_fail(ISO_ERR_NOMEM, "pinned host allocation of %zu bytes failed", want);
+        }
+        ctx->host_pinned = p;
+        ctx->host_pinned_cap = want;
+    }
+    *out = ctx->host_pinned;
+    return ISO_OK;
+}
+
+bool iso_is_device_ptr(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+static std::mutex g_default_mu;
+static iso_ctx *g_default_ctx = nullptr;
+
+iso_ctx *iso_default_ctx()
+{
+    std::lock_guard<std::mutex> lock(g_default_mu);
+    if (!g_default_ctx) {
+        if (iso_ctx_create(0, &g_default_ctx) != ISO_OK) g_default_ctx = nullptr;
+    }
+    return g_default_ctx;
+}

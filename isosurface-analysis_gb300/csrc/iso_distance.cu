@@ -1,0 +1,463 @@
+// iso_distance.cu -- nearest-surface distance fields for many point sets.
+//
+// Replaces generateHierarchy_h / traverse_h and their kernels
+// (isosurfaces_cuda/src/BVH.cu:108-383, 393-706, 814-875).  The sample point of
+// DF index idx (z fastest over the (X/ds, Y/ds, Z/ds) grid) is
+// ((x*ds + ds/2)/X, (y*ds + ds/2)/Y, (z*ds + ds/2)/Z) (BVH.cu:393-406); surface
+// points are normalised by max(X,Y,Z) (funcs.cpp:209-233).  The field value is
+// sqrt(min over points of the canonical squared distance); a one-point surface
+// stores the squared distance, as the reference does (BVH.cu:604-611).
+//
+// Two methods with bit-identical output:
+//  * brute force: each thread owns four samples, points stream through shared
+//    memory in tiles (plain FP32 comparator path);
+//  * LBVH: all point sets at once -- 30-bit Morton codes (BVH.cu:84-117), one
+//    radix sort of (set, code) keys, Karras hierarchy per set with ties broken
+//    by index (exact for duplicate codes), bottom-up boxes with release/acquire
+//    fences, then a stack traversal per sample.  A child box is skipped only if
+//    its canonical box distance is >= the best squared distance so far; the box
+//    distance is the same fma chain over per-axis gaps, which never exceeds the
+//    canonical distance of any point inside (rounding is monotone), so the
+//    minimum equals the brute-force minimum bit for bit.
+#include <cub/cub.cuh>
+
+#include <vector>
+
+#include "iso_internal.cuh"
+
+namespace {
+
+constexpr int BRUTE_THREADS = 256;
+constexpr int BRUTE_SAMPLES = 4;  // per thread
+constexpr int BRUTE_TILE = 1024;  // points per shared-memory tile
+constexpr int QUERY_THREADS = 128;
+constexpr int STACK_DEPTH = 64;
+constexpr float INIT_BOUND = 100000.0f;  // the reference's initial upper bound (BVH.cu:639)
+
+struct SampleGrid {
+    int X, Y, Z, ds;
+    int64_t Y10, Z10, F;
+};
+
+__device__ __forceinline__ float3 sample_point(const SampleGrid &g, int64_t idx)
+{
+    int64_t z = idx % g.Z10, y = (idx / g.Z10) % g.Y10, x = idx / (g.Y10 * g.Z10);
+    float3 s;
+    s.x = __fdiv_rn((float)(x * g.ds + g.ds / 2), (float)g.X);
+    s.y = __fdiv_rn((float)(y * g.ds + g.ds / 2), (float)g.Y);
+    s.z = __fdiv_rn((float)(z * g.ds + g.ds / 2), (float)g.Z);
+    return s;
+}
+
+__device__ __forceinline__ float finish(float best, int64_t P) { return P == 1 ? best : __fsqrt_rn(best); }
+
+struct Segments {
+    const float4 *points;   // normalised points (w unused)
+    const int64_t *offset;  // per segment: first point
+    const int64_t *count;   // per segment: number of points
+};
+
+__global__ void __launch_bounds__(BRUTE_THREADS) df_brute_kernel(Segments sg, SampleGrid g, float *fields,
+                                                                   int64_t stride, int seg_base)
+{
+    __shared__ float4 tile[BRUTE_TILE];
+    const int seg = seg_base + blockIdx.y;
+    const int64_t off = sg.offset[seg], P = sg.count[seg];
+    const int64_t first = (int64_t)blockIdx.x * BRUTE_THREADS * BRUTE_SAMPLES + threadIdx.x;
+    float sx[BRUTE_SAMPLES], sy[BRUTE_SAMPLES], sz[BRUTE_SAMPLES], best[BRUTE_SAMPLES];
+#pragma unroll
+    for (int q = 0; q < BRUTE_SAMPLES; ++q) {
+        int64_t idx = first + (int64_t)q * BRUTE_THREADS;
+        float3 s = sample_point(g, idx < g.F ? idx : g.F - 1);
+        sx[q] = s.x;
+        sy[q] = s.y;
+        sz[q] = s.z;
+        best[q] = INIT_BOUND;
+    }
+    for (int64_t base = 0; base < P; base += BRUTE_TILE) {
+        const int len = (int)(P - base < BRUTE_TILE ? P - base : BRUTE_TILE);
+        __syncthreads();
+        for (int t = threadIdx.x; t < len; t += BRUTE_THREADS) tile[t] = sg.points[off + base + t];
+        __syncthreads();
+#pragma unroll 4
+        for (int t = 0; t < len; ++t) {
+            const float4 p = tile[t];
+#pragma unroll
+            for (int q = 0; q < BRUTE_SAMPLES; ++q) {
+                float d = iso_dist2(__fsub_rn(sx[q], p.x), __fsub_rn(sy[q], p.y), __fsub_rn(sz[q], p.z));
+                best[q] = fminf(best[q], d);
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < BRUTE_SAMPLES; ++q) {
+        int64_t idx = first + (int64_t)q * BRUTE_THREADS;
+        if (idx < g.F) fields[(size_t)blockIdx.y * stride + idx] = finish(best[q], P);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// LBVH
+// ---------------------------------------------------------------------------
+
+struct BvhNode {    // 64 bytes: both child boxes live in the parent
+    float4 l_lo;    // xyz = left box min,  w = left child (int bits)
+    float4 l_hi;    // xyz = left box max,  w = right child (int bits)
+    float4 r_lo;    // xyz = right box min
+    float4 r_hi;    // xyz = right box max
+};
+constexpr int LEAF_BIT = (int)0x80000000;
+
+// Expands a 10-bit integer into 30 bits with two zeros between bits and the
+// 30-bit Morton code of a point in the unit cube, as BVH.cu:84-117 computes it.
+__device__ __forceinline__ unsigned int expand_bits(unsigned int v)
+{
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+__device__ __forceinline__ unsigned int morton30(float x, float y, float z)
+{
+    x = fminf(fmaxf(__fmul_rn(x, 1024.0f), 0.0f), 1023.0f);
+    y = fminf(fmaxf(__fmul_rn(y, 1024.0f), 0.0f), 1023.0f);
+    z = fminf(fmaxf(__fmul_rn(z, 1024.0f), 0.0f), 1023.0f);
+    return expand_bits((unsigned int)x) * 4 + expand_bits((unsigned int)y) * 2 + expand_bits((unsigned int)z);
+}
+
+__device__ __forceinline__ int find_segment(const int64_t *starts, int m, int64_t i)
+{
+    int lo = 0, hi = m - 1;  // last s with starts[s] <= i
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (starts[mid] <= i) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+struct Bvh {
+    const int64_t *cstart;   // per segment: first sorted leaf (compact numbering)
+    const int64_t *ccount;   // per segment: leaves
+    int m;
+    int64_t total;           // all leaves
+    unsigned long long *keys;
+    unsigned int *vals;
+    float4 *compact;         // gathered points, compact numbering
+    float4 *leaves;          // sorted points
+    BvhNode *nodes;          // segment s owns nodes [cstart[s]-s, cstart[s]-s+count-1)
+    int *parent_node;        // per internal node: parent*2 + side, -1 at the root
+    int *parent_leaf;        // per leaf: parent*2 + side, -1 for a one-leaf segment
+    unsigned int *flags;
+    int *error;
+};
+
+__global__ void bvh_keys_kernel(Segments sg, Bvh b)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.total) return;
+    int s = find_segment(b.cstart, b.m, i);
+    float4 p = sg.points[sg.offset[s] + (i - b.cstart[s])];
+    b.compact[i] = p;
+    b.keys[i] = ((unsigned long long)s << 32) | morton30(p.x, p.y, p.z);
+    b.vals[i] = (unsigned int)i;
+}
+
+__global__ void bvh_gather_kernel(Bvh b, const unsigned int *sorted_vals)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.total) return;
+    b.leaves[i] = b.compact[sorted_vals[i]];
+}
+
+// delta of the Karras construction over index-augmented keys
+__device__ __forceinline__ int karras_delta(const unsigned long long *codes, int n, int i, int j)
+{
+    if (j < 0 || j >= n) return -1;
+    unsigned int ci = (unsigned int)codes[i], cj = (unsigned int)codes[j];
+    if (ci == cj) return 32 + __clz(i ^ j);
+    return __clz(ci ^ cj);
+}
+
+__global__ void bvh_build_kernel(Bvh b, const unsigned long long *sorted_keys)
+{
+    int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total_nodes = b.total - b.m;
+    if (g >= total_nodes) return;
+    // segment s owns internal nodes [cstart[s] - s, cstart[s] - s + count[s] - 1)
+    int lo = 0, hi = b.m - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (b.cstart[mid] - mid <= g) lo = mid; else hi = mid - 1;
+    }
+    // one-point segments own no node and share the next segment's base; the
+    // last segment whose base is <= g owns node g
+    const int s = lo;
+    const int64_t nbase = b.cstart[s] - s;
+    const int n = (int)b.ccount[s];
+    const int i = (int)(g - nbase);
+    const unsigned long long *codes = sorted_keys + b.cstart[s];
+
+    int d = karras_delta(codes, n, i, i + 1) - karras_delta(codes, n, i, i - 1) > 0 ? 1 : -1;
+    if (i == 0) d = 1;
+    int dmin = karras_delta(codes, n, i, i - d);
+    int lmax = 2;
+    while (karras_delta(codes, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (karras_delta(codes, n, i, i + (l + t) * d) > dmin) l += t;
+    const int j = i + l * d;
+    const int dnode = karras_delta(codes, n, i, j);
+    int sp = 0;
+    int t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (karras_delta(codes, n, i, i + (sp + t) * d) > dnode) sp += t;
+    } while (t > 1);
+    const int split = i + sp * d + (d < 0 ? -1 : 0);
+    const int first = i < j ? i : j, last = i < j ? j : i;
+    const int left = (first == split) ? (split | LEAF_BIT) : split;
+    const int right = (last == split + 1) ? ((split + 1) | LEAF_BIT) : split + 1;
+
+    BvhNode *node = b.nodes + nbase + i;
+    node->l_lo.w = __int_as_float(left);
+    node->l_hi.w = __int_as_float(right);
+    if (left & LEAF_BIT) b.parent_leaf[b.cstart[s] + (left & ~LEAF_BIT)] = i * 2 + 0;
+    else b.parent_node[nbase + left] = i * 2 + 0;
+    if (right & LEAF_BIT) b.parent_leaf[b.cstart[s] + (right & ~LEAF_BIT)] = i * 2 + 1;
+    else b.parent_node[nbase + right] = i * 2 + 1;
+    if (i == 0) b.parent_node[nbase] = -1;
+}
+
+__device__ __forceinline__ void store_box(BvhNode *node, int side, float3 lo, float3 hi)
+{
+    // keep the child index stored in .w of l_lo / l_hi
+    if (side == 0) {
+        __stcg(&node->l_lo.x, lo.x); __stcg(&node->l_lo.y, lo.y); __stcg(&node->l_lo.z, lo.z);
+        __stcg(&node->l_hi.x, hi.x); __stcg(&node->l_hi.y, hi.y); __stcg(&node->l_hi.z, hi.z);
+    } else {
+        __stcg(&node->r_lo.x, lo.x); __stcg(&node->r_lo.y, lo.y); __stcg(&node->r_lo.z, lo.z);
+        __stcg(&node->r_hi.x, hi.x); __stcg(&node->r_hi.y, hi.y); __stcg(&node->r_hi.z, hi.z);
+    }
+}
+
+__global__ void bvh_boxes_kernel(Bvh b)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.total) return;
+    int s = find_segment(b.cstart, b.m, i);
+    // a segment with one leaf has no internal node
+    if (b.ccount[s] < 2) return;
+    const int64_t nbase = b.cstart[s] - s;
+    float4 p = b.leaves[i];
+    float3 lo = make_float3(p.x, p.y, p.z), hi = lo;
+    int link = b.parent_leaf[i];
+    // depth is bounded by the 62-bit augmented key, the loop by the node count
+    for (int guard = 0; guard < 4096 && link >= 0; ++guard) {
+        const int parent = link >> 1, side = link & 1;
+        BvhNode *node = b.nodes + nbase + parent;
+        store_box(node, side, lo, hi);
+        __threadfence();
+        if (atomicAdd(&b.flags[nbase + parent], 1u) == 0) return;  // sibling not done yet
+        __threadfence();
+        float3 a_lo = make_float3(__ldcg(&node->l_lo.x), __ldcg(&node->l_lo.y), __ldcg(&node->l_lo.z));
+        float3 a_hi = make_float3(__ldcg(&node->l_hi.x), __ldcg(&node->l_hi.y), __ldcg(&node->l_hi.z));
+        float3 c_lo = make_float3(__ldcg(&node->r_lo.x), __ldcg(&node->r_lo.y), __ldcg(&node->r_lo.z));
+        float3 c_hi = make_float3(__ldcg(&node->r_hi.x), __ldcg(&node->r_hi.y), __ldcg(&node->r_hi.z));
+        lo = make_float3(fminf(a_lo.x, c_lo.x), fminf(a_lo.y, c_lo.y), fminf(a_lo.z, c_lo.z));
+        hi = make_float3(fmaxf(a_hi.x, c_hi.x), fmaxf(a_hi.y, c_hi.y), fmaxf(a_hi.z, c_hi.z));
+        link = b.parent_node[nbase + parent];
+    }
+    if (link >= 0) atomicExch(b.error, 1);
+}
+
+// canonical squared distance from s to a box (0 inside)
+__device__ __forceinline__ float box_dist2(float3 s, float3 lo, float3 hi)
+{
+    float gx = fmaxf(fmaxf(__fsub_rn(lo.x, s.x), __fsub_rn(s.x, hi.x)), 0.0f);
+    float gy = fmaxf(fmaxf(__fsub_rn(lo.y, s.y), __fsub_rn(s.y, hi.y)), 0.0f);
+    float gz = fmaxf(fmaxf(__fsub_rn(lo.z, s.z), __fsub_rn(s.z, hi.z)), 0.0f);
+    return iso_dist2(gx, gy, gz);
+}
+
+__global__ void __launch_bounds__(QUERY_THREADS) bvh_query_kernel(Bvh b, SampleGrid g, float *fields, int64_t stride)
+{
+    const int s = blockIdx.y;
+    const int64_t idx = (int64_t)blockIdx.x * QUERY_THREADS + threadIdx.x;
+    if (idx >= g.F) return;
+    const float3 sp = sample_point(g, idx);
+    const int64_t n = b.ccount[s];
+    const float4 *leaves = b.leaves + b.cstart[s];
+    float best = INIT_BOUND;
+    if (n == 1) {
+        float4 p = __ldg(leaves);
+        best = fminf(best, iso_dist2(__fsub_rn(sp.x, p.x), __fsub_rn(sp.y, p.y), __fsub_rn(sp.z, p.z)));
+    } else {
+        const BvhNode *nodes = b.nodes + (b.cstart[s] - s);
+        int stack[STACK_DEPTH];
+        float sdist[STACK_DEPTH];
+        int top = 0;
+        int cur = 0;
+        for (;;) {
+            const float4 a0 = __ldg(&nodes[cur].l_lo), a1 = __ldg(&nodes[cur].l_hi);
+            const float4 c0 = __ldg(&nodes[cur].r_lo), c1 = __ldg(&nodes[cur].r_hi);
+            const int left = __float_as_int(a0.w), right = __float_as_int(a1.w);
+            const float dl = box_dist2(sp, make_float3(a0.x, a0.y, a0.z), make_float3(a1.x, a1.y, a1.z));
+            const float dr = box_dist2(sp, make_float3(c0.x, c0.y, c0.z), make_float3(c1.x, c1.y, c1.z));
+            // a leaf's box is its point: the box distance is its canonical distance
+            bool gl = false, gr = false;
+            if (left & LEAF_BIT) best = fminf(best, dl); else gl = dl < best;
+            if (right & LEAF_BIT) best = fminf(best, dr); else gr = dr < best;
+            if (gl && gr) {
+                const bool lfirst = dl <= dr;
+                if (top == STACK_DEPTH) { atomicExch(b.error, 2); break; }
+                stack[top] = lfirst ? right : left;
+                sdist[top] = lfirst ? dr : dl;
+                ++top;
+                cur = lfirst ? left : right;
+            } else if (gl) {
+                cur = left;
+            } else if (gr) {
+                cur = right;
+            } else {
+                // pop the next postponed subtree that can still improve
+                while (top > 0 && !(sdist[top - 1] < best)) --top;
+                if (top == 0) break;
+                cur = stack[--top];
+            }
+        }
+    }
+    fields[(size_t)s * stride + idx] = finish(best, n);
+}
+
+}  // namespace
+
+// Distance fields of `num_segments` point sets (normalised points in
+// BUF_POINTS_NORM; segment q has h_seg_count[q] points at h_seg_offset[q]) into
+// BUF_FIELDS rows q (stride field_stride floats), then per-field min/max into
+// BUF_FIELD_MINMAX.
+int iso_run_distance(iso_ctx *ctx, int X, int Y, int Z, int ds, int method, const int32_t * /*h_segments*/,
+                     int num_segments, const int64_t *h_seg_offset, const int64_t *h_seg_count, int64_t field_stride)
+{
+    const int m = num_segments;
+    if (m <= 0) return ISO_OK;
+    if (ds < 1 || X / ds < 1 || Y / ds < 1 || Z / ds < 1) return iso_fail(ISO_ERR_ARG, "bad downscale %d", ds);
+    SampleGrid g;
+    g.X = X;
+    g.Y = Y;
+    g.Z = Z;
+    g.ds = ds;
+    g.Y10 = Y / ds;
+    g.Z10 = Z / ds;
+    g.F = (int64_t)(X / ds) * g.Y10 * g.Z10;
+    for (int q = 0; q < m; ++q)
+        if (h_seg_count[q] < 1) return iso_fail(ISO_ERR_ARG, "distance field of an empty surface");
+
+    void *d_off, *d_cnt, *d_fields, *d_minmax;
+    ISO_TRY(iso_buf(ctx, BUF_SEG_OFFSET, (size_t)m * sizeof(int64_t), &d_off));
+    ISO_TRY(iso_buf(ctx, BUF_SEG_COUNT, (size_t)m * sizeof(int64_t), &d_cnt));
+    ISO_TRY(iso_buf(ctx, BUF_FIELDS, (size_t)m * field_stride * sizeof(float), &d_fields));
+    ISO_TRY(iso_buf(ctx, BUF_FIELD_MINMAX, (size_t)m * 2 * sizeof(uint32_t), &d_minmax));
+    ISO_CUDA(cudaMemcpyAsync(d_off, h_seg_offset, m * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    ISO_CUDA(cudaMemcpyAsync(d_cnt, h_seg_count, m * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    Segments sg;
+    sg.points = (const float4 *)ctx->buf[BUF_POINTS_NORM];
+    sg.offset = (const int64_t *)d_off;
+    sg.count = (const int64_t *)d_cnt;
+    float *fields = (float *)d_fields;
+
+    if (method == ISO_DF_BRUTE) {
+        const int64_t per_block = (int64_t)BRUTE_THREADS * BRUTE_SAMPLES;
+        const unsigned bx = (unsigned)((g.F + per_block - 1) / per_block);
+        for (int base = 0; base < m; base += 65535) {
+            int cnt = m - base < 65535 ? m - base : 65535;
+            df_brute_kernel<<<dim3(bx, cnt), BRUTE_THREADS, 0, ctx->stream>>>(sg, g, fields + (size_t)base * field_stride,
+                                                                             field_stride, base);
+            ISO_LAUNCHED(ctx);
+        }
+    } else if (method == ISO_DF_LBVH) {
+        std::vector<int64_t> cstart(m);
+        int64_t total = 0;
+        for (int q = 0; q < m; ++q) {
+            cstart[q] = total;
+            total += h_seg_count[q];
+        }
+        if (total >= (int64_t)0x7fffffff) return iso_fail(ISO_ERR_CAPACITY, "too many surface points (%lld)", (long long)total);
+        void *d_cstart, *d_keys, *d_keys2, *d_vals, *d_vals2, *d_compact, *d_leaves, *d_nodes, *d_pn, *d_pl, *d_flags, *d_misc;
+        ISO_TRY(iso_buf(ctx, BUF_STAGING_A, (size_t)m * 2 * sizeof(int64_t), &d_cstart));
+        ISO_TRY(iso_buf(ctx, BUF_SORT_KEYS, (size_t)total * 8, &d_keys));
+        ISO_TRY(iso_buf(ctx, BUF_SORT_KEYS_ALT, (size_t)total * 8, &d_keys2));
+        ISO_TRY(iso_buf(ctx, BUF_SORT_VALS, (size_t)total * 4, &d_vals));
+        ISO_TRY(iso_buf(ctx, BUF_SORT_VALS_ALT, (size_t)total * 4, &d_vals2));
+        ISO_TRY(iso_buf(ctx, BUF_STAGING_B, (size_t)total * sizeof(float4), &d_compact));
+        ISO_TRY(iso_buf(ctx, BUF_BVH_LEAVES, (size_t)total * sizeof(float4), &d_leaves));
+        ISO_TRY(iso_buf(ctx, BUF_BVH_NODES, (size_t)total * sizeof(BvhNode), &d_nodes));
+        ISO_TRY(iso_buf(ctx, BUF_BVH_PARENT, (size_t)total * 2 * sizeof(int), &d_pn));
+        ISO_TRY(iso_buf(ctx, BUF_BVH_FLAGS, (size_t)total * sizeof(unsigned int), &d_flags));
+        ISO_TRY(iso_buf(ctx, BUF_MISC, 256, &d_misc));
+        d_pl = (int *)d_pn + total;
+        std::vector<int64_t> cs2(2 * (size_t)m);
+        for (int q = 0; q < m; ++q) {
+            cs2[q] = cstart[q];
+            cs2[m + q] = h_seg_count[q];
+        }
+        ISO_CUDA(cudaMemcpyAsync(d_cstart, cs2.data(), cs2.size() * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+        ISO_CUDA(cudaMemsetAsync(d_flags, 0, (size_t)total * sizeof(unsigned int), ctx->stream));
+        ISO_CUDA(cudaMemsetAsync(d_misc, 0, sizeof(int), ctx->stream));
+        Bvh b;
+        b.cstart = (const int64_t *)d_cstart;
+        b.ccount = (const int64_t *)d_cstart + m;
+        b.m = m;
+        b.total = total;
+        b.keys = (unsigned long long *)d_keys;
+        b.vals = (unsigned int *)d_vals;
+        b.compact = (float4 *)d_compact;
+        b.leaves = (float4 *)d_leaves;
+        b.nodes = (BvhNode *)d_nodes;
+        b.parent_node = (int *)d_pn;
+        b.parent_leaf = (int *)d_pl;
+        b.flags = (unsigned int *)d_flags;
+        b.error = (int *)d_misc;
+        const unsigned tb = (unsigned)((total + 255) / 256);
+        bvh_keys_kernel<<<tb, 256, 0, ctx->stream>>>(sg, b);
+        ISO_LAUNCHED(ctx);
+        int end_bit = 32;
+        while ((1ll << (end_bit - 32)) < m && end_bit < 64) ++end_bit;
+        cub::DoubleBuffer<unsigned long long> kb((unsigned long long *)d_keys, (unsigned long long *)d_keys2);
+        cub::DoubleBuffer<unsigned int> vb((unsigned int *)d_vals, (unsigned int *)d_vals2);
+        size_t temp_bytes = 0;
+        ISO_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, kb, vb, (int)total, 0, end_bit, ctx->stream));
+        void *d_temp;
+        ISO_TRY(iso_buf(ctx, BUF_CUB_TEMP, temp_bytes, &d_temp));
+        ISO_CUDA(cub::DeviceRadixSort::SortPairs(d_temp, temp_bytes, kb, vb, (int)total, 0, end_bit, ctx->stream));
+        ctx->launches += 4;
+        bvh_gather_kernel<<<tb, 256, 0, ctx->stream>>>(b, vb.Current());
+        ISO_LAUNCHED(ctx);
+        const int64_t total_nodes = total - m;
+        if (total_nodes > 0) {
+            bvh_build_kernel<<<(unsigned)((total_nodes + 255) / 256), 256, 0, ctx->stream>>>(b, kb.Current());
+            ISO_LAUNCHED(ctx);
+            bvh_boxes_kernel<<<tb, 256, 0, ctx->stream>>>(b);
+            ISO_LAUNCHED(ctx);
+        }
+        for (int base = 0; base < m; base += 65535) {
+            int cnt = m - base < 65535 ? m - base : 65535;
+            Bvh bb = b;
+            bb.cstart = b.cstart + base;
+            bb.ccount = b.ccount + base;
+            // node bases are cstart[s] - s with the global s: shift nodes accordingly
+            bb.nodes = b.nodes - base;
+            bvh_query_kernel<<<dim3((unsigned)((g.F + QUERY_THREADS - 1) / QUERY_THREADS), cnt), QUERY_THREADS, 0,
+                               ctx->stream>>>(bb, g, fields + (size_t)base * field_stride, field_stride);
+            ISO_LAUNCHED(ctx);
+        }
+        int err = 0;
+        ISO_CUDA(cudaMemcpyAsync(&err, d_misc, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        ISO_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (err) return iso_fail(ISO_ERR_INTERNAL, "LBVH consistency check failed (code %d)", err);
+    } else {
+        return iso_fail(ISO_ERR_ARG, "unknown distance-field method %d", method);
+    }
+    return iso_run_minmax(ctx, fields, m, g.F, field_stride, (uint32_t *)d_minmax);
+}

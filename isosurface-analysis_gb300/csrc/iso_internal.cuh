@@ -1,0 +1,139 @@
+// iso_internal.cuh -- shared internals of the GB300 isosurface-similarity engine:
+// context, device arena, error reporting and the exact FP32 primitives every
+// kernel uses.  All kernels are compiled with -fmad=false: no multiply-add is
+// fused unless written as __fmaf_rn, so device results match the CPU rounding
+// step for step.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <cstdio>
+
+#include "isosim.h"
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+int iso_fail(int code, const char *fmt, ...);
+void iso_clear_error();
+
+#define ISO_CUDA(call)                                                                     \
+    do {                                                                                   \
+        cudaError_t e__ = (call);                                                          \
+        if (e__ != cudaSuccess)                                                            \
+            return iso_fail(e__ == cudaErrorMemoryAllocation ? ISO_ERR_NOMEM : ISO_ERR_CUDA, \
+                            "%s:%d: %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e__)); \
+    } while (0)
+
+#define ISO_TRY(expr)                 \
+    do {                              \
+        int s__ = (expr);             \
+        if (s__ != ISO_OK) return s__; \
+    } while (0)
+
+#define ISO_LAUNCHED(ctx)                                                                  \
+    do {                                                                                   \
+        (ctx)->launches++;                                                                 \
+        cudaError_t e__ = cudaGetLastError();                                              \
+        if (e__ != cudaSuccess)                                                            \
+            return iso_fail(ISO_ERR_CUDA, "%s:%d: launch failed: %s", __FILE__, __LINE__,   \
+                            cudaGetErrorString(e__));                                      \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// device arena: named grow-only buffers owned by a context
+// ---------------------------------------------------------------------------
+enum IsoBuf {
+    BUF_VOLUME = 0,
+    BUF_ISO_SORTED,
+    BUF_ISO_ORDER,
+    BUF_SURF_COUNTS,     // per sorted isovalue: [regular, corner candidates, active, total verts]
+    BUF_SURF_CURSOR,
+    BUF_POINTS_RAW,      // float4 raw positions (grid units), all isovalues
+    BUF_POINTS_NORM,     // float4 normalised positions
+    BUF_CORNER_KEYS,
+    BUF_CORNER_KEYS_ALT,
+    BUF_SEG_OFFSET,      // per segment: first point (int64)
+    BUF_SEG_COUNT,       // per segment: point count (int64)
+    BUF_SORT_KEYS,
+    BUF_SORT_KEYS_ALT,
+    BUF_SORT_VALS,
+    BUF_SORT_VALS_ALT,
+    BUF_BVH_NODES,
+    BUF_BVH_PARENT,
+    BUF_BVH_FLAGS,
+    BUF_BVH_LEAVES,
+    BUF_FIELDS,          // distance fields, m x field_stride floats
+    BUF_FIELD_MINMAX,    // per field: uint32 bits of min and max
+    BUF_PAIR_TASKS,
+    BUF_HIST_SCRATCH,    // per CTA: bins*bins uint32
+    BUF_ISM,
+    BUF_TASK_COUNTER,
+    BUF_HIST_DUMP,
+    BUF_MISC,
+    BUF_CUB_TEMP,
+    BUF_STAGING_A,
+    BUF_STAGING_B,
+    BUF_COUNT_
+};
+
+struct iso_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    void *buf[BUF_COUNT_] = {};
+    size_t cap[BUF_COUNT_] = {};
+    int64_t launches = 0;
+    void *host_pinned = nullptr;
+    size_t host_pinned_cap = 0;
+};
+
+// Ensures buffer `b` holds at least `bytes`; contents are not preserved.
+int iso_buf(iso_ctx *ctx, IsoBuf b, size_t bytes, void **out);
+// Pinned host scratch of at least `bytes`.
+int iso_host_scratch(iso_ctx *ctx, size_t bytes, void **out);
+
+// Process-wide context for the reference-named entry points.
+iso_ctx *iso_default_ctx();
+
+// True if `p` is a device (or managed) pointer.
+bool iso_is_device_ptr(const void *p);
+
+// ---------------------------------------------------------------------------
+// exact FP32 primitives
+// ---------------------------------------------------------------------------
+
+// Canonical squared distance: fma(dz,dz, fma(dy,dy, dx*dx)), each step rounded
+// once.  The CPU oracle uses the same expression with libm fmaf.
+__device__ __forceinline__ float iso_dist2(float dx, float dy, float dz)
+{
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// Bucket of isosurfaces_cuda/src/JointHistogram.cu:63-75 with IEEE division.
+// Values below the interval (only possible with a caller-supplied interval that
+// does not contain the data) go to bucket 0 instead of indexing out of bounds.
+__device__ __forceinline__ int iso_bucket(float v, float mn, float step, int bins)
+{
+    if (step == 0.0f) return 0;
+    int b = __float2int_rz(__fdiv_rn(__fsub_rn(v, mn), step));
+    b = b >= bins ? bins - 1 : b;
+    return b < 0 ? 0 : b;
+}
+
+// Host-side launch helpers implemented per stage.
+int iso_run_surfaces(iso_ctx *ctx, const float *d_vol, int X, int Y, int Z, const float *h_iso, int n,
+                     int surface, int frame, int64_t *h_counts, int64_t *h_offsets,
+                     iso_surface_stats *h_stats, int64_t *total_points_out);
+int iso_run_distance(iso_ctx *ctx, int X, int Y, int Z, int ds, int method, const int32_t *h_segments,
+                     int num_segments, const int64_t *h_seg_offset, const int64_t *h_seg_count,
+                     int64_t field_stride);
+int iso_run_similarity(iso_ctx *ctx, const float *d_fields_a, const float *d_fields_b, int m,
+                       int64_t n, int64_t stride, int bins, const uint32_t *d_minmax_a,
+                       const uint32_t *d_minmax_b, float *d_ism, uint32_t *d_joint_dump,
+                       uint32_t *d_colrow_dump);
+int iso_run_minmax(iso_ctx *ctx, const float *d_fields, int m, int64_t n, int64_t stride, uint32_t *d_minmax);
+
+constexpr int ISO_MAX_BINS = 256;
+constexpr int ISO_MAX_ISOVALUES = 4096;

@@ -1,0 +1,96 @@
+"""Joint histograms and NMI on the GPU against the oracle and the reference's
+golden vectors.  Bin counts are bit-exact; the FP64 NMI matches the oracle's
+FP64 NMI to float rounding and the reference's FP32 NMI within its own FP32
+rounding noise (ISM tolerance 2e-5, the largest FP32-vs-FP64 gap the
+reference's arithmetic shows on these inputs)."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+TOL_F64 = 1e-6   # FP64 NMI rounded to float, different summation order
+TOL_REF = 2e-5   # vs the reference's FP32 NMI
+
+
+def fields_like_df(m, n, seed):
+    rng = np.random.default_rng(seed)
+    base = rng.uniform(0, 1, n)
+    return np.stack([np.abs(base * (1 + 0.25 * k) + 0.15 * rng.standard_normal(n)) for k in range(m)]).astype(np.float32)
+
+
+def test_golden_small_reference_named_entry():
+    import isosim
+    g = np.load(os.path.join(GOLDEN, "simmap_small.npz"))
+    fields, bins = g["fields"], int(g["bins"])
+    mins = [oracle.field_interval(f)[0] for f in fields]
+    maxs = [oracle.field_interval(f)[1] for f in fields]
+    sim, cols, rows = isosim.calculate_histogram_h(list(fields), mins, maxs, bins)
+    assert np.array_equal(cols, g["cols"])
+    assert np.array_equal(rows, g["rows"])
+    assert np.abs(sim - g["sim"]).max() < TOL_REF
+
+
+@pytest.mark.parametrize("m,n,bins", [(6, 300001, 256), (9, 70001, 128), (3, 4097, 32), (2, 5, 16)])
+def test_joint_histograms_bit_exact(ctx, m, n, bins):
+    f = fields_like_df(m, n, seed=m * 7 + bins)
+    ism, joint = ctx.similarity_map(f, bins, joint=True)
+    for i in range(m):
+        for j in range(m):
+            want, _, _ = oracle.pair_histogram(f[i], f[j], bins)
+            assert np.array_equal(joint[i, j], want), (i, j)
+    want = oracle.similarity_map(f, bins, mode=0)
+    assert np.abs(ism - want).max() < TOL_F64
+    assert np.array_equal(ism, ism.T)
+
+
+def test_against_reference_fp32(ctx, ref):
+    f = fields_like_df(5, 200003, seed=3)
+    ism = ctx.similarity_map(f, 128)
+    want = oracle.ref_similarity_map(ref, list(f), 128)
+    assert np.abs(ism - want).max() < TOL_REF
+
+
+def test_constant_and_degenerate_fields(ctx):
+    n = 10000
+    f = np.stack([np.full(n, 0.25, np.float32), np.zeros(n, np.float32),
+                  np.linspace(0, 1, n).astype(np.float32)])
+    ism, joint = ctx.similarity_map(f, 64, joint=True)
+    for i in range(3):
+        for j in range(3):
+            want, _, _ = oracle.pair_histogram(f[i], f[j], 64)
+            assert np.array_equal(joint[i, j], want)
+    want = oracle.similarity_map(f, 64, mode=0)
+    assert np.abs(ism - want).max() < TOL_F64
+
+
+def test_cross_map_and_multi_entry(ctx):
+    import isosim
+    a = fields_like_df(4, 50021, seed=11)
+    b = fields_like_df(4, 50021, seed=12) * 1.5
+    cm = ctx.cross_map(a, b, 64)
+    for i in range(4):
+        for j in range(4):
+            lo_i, hi_i = oracle.field_interval(a[i])
+            lo_j, hi_j = oracle.field_interval(b[j])
+            joint, _, _ = oracle.pair_histogram(a[i], b[j], 64, (lo_i, hi_i), (lo_j, hi_j))
+            assert abs(cm[i, j] - oracle.mi_f64(joint, a.shape[1])) < TOL_F64
+    fields = list(a) + list(b)
+    mins = [oracle.field_interval(x)[0] for x in fields]
+    maxs = [oracle.field_interval(x)[1] for x in fields]
+    sim, cols, rows = isosim.calculate_histogram_h(fields, mins, maxs, 64, multi=True)
+    assert np.abs(sim - cm).max() < TOL_F64
+    for i in range(4):
+        for j in range(4):
+            joint, cs, rs = oracle.pair_histogram(a[i], b[j], 64, (mins[i], maxs[i]), (mins[4 + j], maxs[4 + j]))
+            assert np.array_equal(cols[i, j], cs) and np.array_equal(rows[i, j], rs)
+
+
+def test_deterministic(ctx):
+    f = fields_like_df(7, 123457, seed=21)
+    a = ctx.similarity_map(f, 256)
+    b = ctx.similarity_map(f, 256)
+    assert np.array_equal(a, b)
