@@ -332,6 +332,28 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_case(case):
+    """Small fixed workloads for kernel profiles: 'hist-small' = similarity
+    map of 16 distance-like fields of 128^3 values at 256 bins; 'pipe-small' =
+    the 64^3, 32-isovalue, 128-bin pipeline."""
+    import isosim
+    import isosim.synth as synth
+    ctx = isosim.Context(0)
+    if case == "hist-small":
+        rng = np.random.default_rng(0)
+        n = 128 ** 3
+        base = rng.uniform(0, 1, n)
+        f = np.stack([np.abs(base * (1 + 0.25 * k) + 0.15 * rng.standard_normal(n)) for k in range(16)]).astype(np.float32)
+        for _ in range(2):
+            ctx.similarity_map(f, 256)
+    else:
+        vol, isos, bins = synth.config1()
+        for _ in range(2):
+            ctx.ism(vol.ravel(), (64, 64, 64), isos, bins=bins)
+    ctx.close()
+    print("case", case, "ok")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -342,8 +364,12 @@ def main():
     ap.add_argument("--df", default="lbvh", choices=["lbvh", "brute"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-scale", type=float, default=1.0)
+    ap.add_argument("--case", default=None, choices=["hist-small", "pipe-small"],
+                    help="run a small fixed case twice and exit (profiling target)")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.case:
+        run_case(args.case)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -281,54 +281,149 @@ __device__ __forceinline__ float box_dist2(float3 s, float3 lo, float3 hi)
     return iso_dist2(gx, gy, gz);
 }
 
+// Query layout: a warp owns an 8 (z) x 4 (y) patch of sample columns and each
+// thread sweeps RUN_X consecutive samples along x.  A block stacks four warps
+// in y, covering 16 (y) x 8 (z) x RUN_X (x) samples.  The nearest point of one
+// sample seeds the next sample's bound (its canonical distance to that real
+// point), which keeps the traversal exact and prunes almost everything but
+// the nearest region.
+constexpr int PATCH_Z = 8, PATCH_Y = 4, WARPS_Y = QUERY_THREADS / 32, RUN_X = 8;
+
+__device__ __forceinline__ void load_node(const BvhNode *nodes, int cur, float4 &a0, float4 &a1, float4 &c0, float4 &c1)
+{
+    a0 = __ldg(&nodes[cur].l_lo);
+    a1 = __ldg(&nodes[cur].l_hi);
+    c0 = __ldg(&nodes[cur].r_lo);
+    c1 = __ldg(&nodes[cur].r_hi);
+}
+
+// Exact nearest canonical squared distance from sp, starting from bound `best`
+// attained at point bp; returns the minimum and updates bp to its point.
+__device__ __forceinline__ float traverse(const BvhNode *nodes, float3 sp, float best, float3 &bp, int *error)
+{
+    int stack[STACK_DEPTH];
+    float sdist[STACK_DEPTH];
+    int top = 0;
+    int cur = 0;
+    for (;;) {
+        float4 a0, a1, c0, c1;
+        load_node(nodes, cur, a0, a1, c0, c1);
+        const int left = __float_as_int(a0.w), right = __float_as_int(a1.w);
+        const float dl = box_dist2(sp, make_float3(a0.x, a0.y, a0.z), make_float3(a1.x, a1.y, a1.z));
+        const float dr = box_dist2(sp, make_float3(c0.x, c0.y, c0.z), make_float3(c1.x, c1.y, c1.z));
+        // a leaf's box is its point: the box distance is its canonical distance
+        bool gl = false, gr = false;
+        if (left & LEAF_BIT) {
+            if (dl < best) {
+                best = dl;
+                bp = make_float3(a0.x, a0.y, a0.z);
+            }
+        } else {
+            gl = dl < best;
+        }
+        if (right & LEAF_BIT) {
+            if (dr < best) {
+                best = dr;
+                bp = make_float3(c0.x, c0.y, c0.z);
+            }
+        } else {
+            gr = dr < best;
+        }
+        if (gl && gr) {
+            const bool lfirst = dl <= dr;
+            if (top == STACK_DEPTH) {
+                atomicExch(error, 2);
+                break;
+            }
+            stack[top] = lfirst ? right : left;
+            sdist[top] = lfirst ? dr : dl;
+            ++top;
+            cur = lfirst ? left : right;
+        } else if (gl) {
+            cur = left;
+        } else if (gr) {
+            cur = right;
+        } else {
+            // pop the next postponed subtree that can still improve
+            while (top > 0 && !(sdist[top - 1] < best)) --top;
+            if (top == 0) break;
+            cur = stack[--top];
+        }
+    }
+    return best;
+}
+
 __global__ void __launch_bounds__(QUERY_THREADS) bvh_query_kernel(Bvh b, SampleGrid g, float *fields, int64_t stride)
 {
     const int s = blockIdx.y;
-    const int64_t idx = (int64_t)blockIdx.x * QUERY_THREADS + threadIdx.x;
-    if (idx >= g.F) return;
-    const float3 sp = sample_point(g, idx);
+    const int64_t X10 = g.F / (g.Y10 * g.Z10);
+    const int64_t nbz = (g.Z10 + PATCH_Z - 1) / PATCH_Z;
+    const int64_t nby = (g.Y10 + PATCH_Y * WARPS_Y - 1) / (PATCH_Y * WARPS_Y);
+    const int64_t tile = blockIdx.x;
+    const int64_t tz = tile % nbz, ty = (tile / nbz) % nby, tx = tile / (nbz * nby);
+    const int lz = threadIdx.x % PATCH_Z, ly = threadIdx.x / PATCH_Z;  // ly in [0, 16)
+    const int64_t z = tz * PATCH_Z + lz, y = ty * PATCH_Y * WARPS_Y + ly, x0 = tx * RUN_X;
+    const bool col_valid = z < g.Z10 && y < g.Y10;
     const int64_t n = b.ccount[s];
     const float4 *leaves = b.leaves + b.cstart[s];
-    float best = INIT_BOUND;
+    float *out = fields + (size_t)s * stride;
+
     if (n == 1) {
-        float4 p = __ldg(leaves);
-        best = fminf(best, iso_dist2(__fsub_rn(sp.x, p.x), __fsub_rn(sp.y, p.y), __fsub_rn(sp.z, p.z)));
-    } else {
-        const BvhNode *nodes = b.nodes + (b.cstart[s] - s);
-        int stack[STACK_DEPTH];
-        float sdist[STACK_DEPTH];
-        int top = 0;
-        int cur = 0;
-        for (;;) {
-            const float4 a0 = __ldg(&nodes[cur].l_lo), a1 = __ldg(&nodes[cur].l_hi);
-            const float4 c0 = __ldg(&nodes[cur].r_lo), c1 = __ldg(&nodes[cur].r_hi);
-            const int left = __float_as_int(a0.w), right = __float_as_int(a1.w);
-            const float dl = box_dist2(sp, make_float3(a0.x, a0.y, a0.z), make_float3(a1.x, a1.y, a1.z));
-            const float dr = box_dist2(sp, make_float3(c0.x, c0.y, c0.z), make_float3(c1.x, c1.y, c1.z));
-            // a leaf's box is its point: the box distance is its canonical distance
-            bool gl = false, gr = false;
-            if (left & LEAF_BIT) best = fminf(best, dl); else gl = dl < best;
-            if (right & LEAF_BIT) best = fminf(best, dr); else gr = dr < best;
-            if (gl && gr) {
-                const bool lfirst = dl <= dr;
-                if (top == STACK_DEPTH) { atomicExch(b.error, 2); break; }
-                stack[top] = lfirst ? right : left;
-                sdist[top] = lfirst ? dr : dl;
-                ++top;
-                cur = lfirst ? left : right;
-            } else if (gl) {
-                cur = left;
-            } else if (gr) {
-                cur = right;
-            } else {
-                // pop the next postponed subtree that can still improve
-                while (top > 0 && !(sdist[top - 1] < best)) --top;
-                if (top == 0) break;
-                cur = stack[--top];
-            }
+        const float4 p = __ldg(leaves);
+        for (int k = 0; k < RUN_X; ++k) {
+            const int64_t x = x0 + k;
+            if (!col_valid || x >= X10) break;
+            const int64_t idx = (x * g.Y10 + y) * g.Z10 + z;
+            const float3 sp = sample_point(g, idx);
+            out[idx] = fminf(INIT_BOUND, iso_dist2(__fsub_rn(sp.x, p.x), __fsub_rn(sp.y, p.y), __fsub_rn(sp.z, p.z)));
+        }
+        return;
+    }
+    const BvhNode *nodes = b.nodes + (b.cstart[s] - s);
+
+    // first sample of the run: greedy descent to a leaf, then the greedy points
+    // of five warp neighbours as further candidates (all lanes take part)
+    int64_t idx0 = col_valid && x0 < X10 ? (x0 * g.Y10 + y) * g.Z10 + z : 0;
+    float3 sp = sample_point(g, idx0);
+    int cur = 0, leaf = 0;
+    for (int depth = 0; depth < STACK_DEPTH; ++depth) {
+        float4 a0, a1, c0, c1;
+        load_node(nodes, cur, a0, a1, c0, c1);
+        const float dl = box_dist2(sp, make_float3(a0.x, a0.y, a0.z), make_float3(a1.x, a1.y, a1.z));
+        const float dr = box_dist2(sp, make_float3(c0.x, c0.y, c0.z), make_float3(c1.x, c1.y, c1.z));
+        const int next = dl <= dr ? __float_as_int(a0.w) : __float_as_int(a1.w);
+        if (next & LEAF_BIT) {
+            leaf = next & ~LEAF_BIT;
+            break;
+        }
+        cur = next;
+    }
+    const float4 gp = __ldg(leaves + leaf);
+    float best = INIT_BOUND;
+    float3 bp = make_float3(gp.x, gp.y, gp.z);
+#pragma unroll
+    for (int o = 0; o < 6; ++o) {
+        const int mask = o == 0 ? 0 : (1 << (o - 1));
+        const float px = __shfl_xor_sync(0xffffffffu, gp.x, mask);
+        const float py = __shfl_xor_sync(0xffffffffu, gp.y, mask);
+        const float pz = __shfl_xor_sync(0xffffffffu, gp.z, mask);
+        const float d = iso_dist2(__fsub_rn(sp.x, px), __fsub_rn(sp.y, py), __fsub_rn(sp.z, pz));
+        if (d < best) {
+            best = d;
+            bp = make_float3(px, py, pz);
         }
     }
-    fields[(size_t)s * stride + idx] = finish(best, n);
+    for (int k = 0; k < RUN_X; ++k) {
+        const int64_t x = x0 + k;
+        if (!col_valid || x >= X10) break;
+        const int64_t idx = (x * g.Y10 + y) * g.Z10 + z;
+        if (k > 0) {
+            sp = sample_point(g, idx);
+            best = iso_dist2(__fsub_rn(sp.x, bp.x), __fsub_rn(sp.y, bp.y), __fsub_rn(sp.z, bp.z));
+        }
+        best = traverse(nodes, sp, best, bp, b.error);
+        out[idx] = __fsqrt_rn(best);
+    }
 }
 
 }  // namespace
@@ -448,8 +543,10 @@ int iso_run_distance(iso_ctx *ctx, int X, int Y, int Z, int ds, int method, cons
             bb.ccount = b.ccount + base;
             // node bases are cstart[s] - s with the global s: shift nodes accordingly
             bb.nodes = b.nodes - base;
-            bvh_query_kernel<<<dim3((unsigned)((g.F + QUERY_THREADS - 1) / QUERY_THREADS), cnt), QUERY_THREADS, 0,
-                               ctx->stream>>>(bb, g, fields + (size_t)base * field_stride, field_stride);
+            const int64_t X10 = X / ds;
+            const int64_t bricks = ((X10 + 7) / 8) * ((g.Y10 + 15) / 16) * ((g.Z10 + 7) / 8);
+            bvh_query_kernel<<<dim3((unsigned)bricks, cnt), QUERY_THREADS, 0, ctx->stream>>>(
+                bb, g, fields + (size_t)base * field_stride, field_stride);
             ISO_LAUNCHED(ctx);
         }
         int err = 0;

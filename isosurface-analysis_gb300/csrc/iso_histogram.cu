@@ -22,8 +22,8 @@
 
 namespace {
 
-constexpr int HIST_THREADS = 512;
-constexpr int HIST_ITERS_PER_FLUSH = 31;  // 31 * 512 threads * 4 voxels = 63488 < 65536
+constexpr int HIST_THREADS = 1024;
+constexpr float BUCKET_TOL = 1.220703125e-4f;  // 2^-13, see fast_bucket
 
 __device__ __forceinline__ float bits_to_float(uint32_t b) { return __uint_as_float(b); }
 
@@ -40,58 +40,194 @@ struct PairArgs {
     int bins;
     int symmetric;        // write (j,i) too
     float *ism;
-    uint32_t *scratch;    // per CTA bins*bins uint32 (zero on entry, left zero)
+    int4 *events;         // per CTA: event_cap wrap events {bin, delta, c16, corr}
+    int event_cap;
+    const double *clnc;   // c*ln(c) for c < 65536
     unsigned int *counter;
+    int *error;
     uint32_t *joint_dump; // optional: m*m*bins*bins
     uint32_t *colrow_dump;// optional: [2][m*m*bins] (col sums, row sums) per ordered pair
 };
 
-__device__ __forceinline__ void count_bin(uint32_t *hist_words, int bin)
+struct Binner {
+    float mn, step, r;
+    int bins;
+    int mode;  // 0: reciprocal with exact fallback, 1: exact division only, 2: step == 0
+};
+
+// Exact bucket of JointHistogram.cu:63-75 (IEEE division), clamped to [0, bins).
+__device__ __forceinline__ int exact_bucket(const Binner &b, float v) { return iso_bucket(v, b.mn, b.step, b.bins); }
+
+// Out of line: the exact path is rare and would otherwise cost registers in the
+// streaming loop.
+__device__ __noinline__ int2 exact_bucket_pair(float mn, float step, int bins, float va, float vb)
 {
-    atomicAdd(&hist_words[bin >> 1], 1u << ((bin & 1) << 4));
+    return make_int2(iso_bucket(va, mn, step, bins), iso_bucket(vb, mn, step, bins));
 }
 
-__device__ void flush_packed(uint32_t *hist_words, int words, uint32_t *global_hist)
+// Both buckets of one voxel through a reciprocal.  q' = RN(RN(v-mn) * RN(1/step))
+// is within 257 * 2^-23 + 2^-15 < 2^-13.5 of RN((v-mn)/step) for q < 257, so
+// floor(q') is the exact bucket unless q' lies within 2^-13 of an integer
+// boundary in [1, bins-1]; then both values take the exact division.  RN(q')
+// comes from adding 1.5 * 2^23 (its integer part lands in the low mantissa
+// bits), which needs q' < 2^22: q' is clamped there first.
+__device__ __forceinline__ void fast_bucket_pair(const Binner &b, float va, float vb, int &ka, int &kb)
 {
-    uint2 *g2 = reinterpret_cast<uint2 *>(global_hist);
-    for (int w = threadIdx.x; w < words; w += blockDim.x) {
-        uint32_t v = hist_words[w];
-        if (v) {
-            uint2 g = g2[w];
-            g.x += v & 0xffffu;
-            g.y += v >> 16;
-            g2[w] = g;
-            hist_words[w] = 0;
+    constexpr float MAGIC = 12582912.0f;  // 1.5 * 2^23
+    constexpr int MAGIC_BITS = 0x4B400000;
+    const float qa = fminf(__fmul_rn(__fsub_rn(va, b.mn), b.r), 2097152.0f);
+    const float qb = fminf(__fmul_rn(__fsub_rn(vb, b.mn), b.r), 2097152.0f);
+    const float ma = __fadd_rn(qa, MAGIC), mb = __fadd_rn(qb, MAGIC);
+    const float da = __fsub_rn(qa, __fsub_rn(ma, MAGIC)), db = __fsub_rn(qb, __fsub_rn(mb, MAGIC));
+    const int ra = __float_as_int(ma) - MAGIC_BITS, rb = __float_as_int(mb) - MAGIC_BITS;  // RN(q')
+    const unsigned inner = (unsigned)(b.bins - 1);
+    const bool slow = (fabsf(da) < BUCKET_TOL && (unsigned)(ra - 1) < inner) ||
+                      (fabsf(db) < BUCKET_TOL && (unsigned)(rb - 1) < inner);
+    // floor(q') = RN(q') - (q' < RN(q')); unsigned min keeps any index in range
+    ka = (int)min((unsigned)(ra - (da < 0.0f)), inner);
+    kb = (int)min((unsigned)(rb - (db < 0.0f)), inner);
+    if (slow) {
+        const int2 e = exact_bucket_pair(b.mn, b.step, b.bins, va, vb);
+        ka = e.x;
+        kb = e.y;
+    }
+}
+
+// Counts one bin as a 16-bit half of a shared 32-bit word.  The returned old
+// word tells this thread exactly when a half wraps: the low half's 16 bits
+// advance only by its own increments, the high half's by its increments plus
+// the low half's carries.  Wraps are logged as corrections:
+//   low half wraps  -> low bin +65536, high bin -1 (the carry it received)
+//   high half wraps -> high bin +65536
+__device__ __noinline__ void log_wrap(int bin, uint32_t sh, uint32_t old, int4 *ev, int cap, unsigned int *nev,
+                                     int *error)
+{
+    const int lo = bin & ~1, hi = bin | 1;
+    const bool both = sh == 0 && (old >> 16) == 0xffffu;
+    const unsigned int ne = sh == 0 ? (both ? 3u : 2u) : 1u;
+    const unsigned int slot = atomicAdd(nev, ne);
+    if (slot + ne > (unsigned int)cap) {
+        atomicExch(error, 3);
+        return;
+    }
+    if (sh == 0) {
+        ev[slot] = make_int4(lo, 65536, 0, 0);
+        ev[slot + 1] = make_int4(hi, -1, 0, 0);
+        if (both) ev[slot + 2] = make_int4(hi, 65536, 0, 0);
+    } else {
+        ev[slot] = make_int4(hi, 65536, 0, 0);
+    }
+}
+
+__device__ __forceinline__ void count_bin(uint32_t *words, int bin, int4 *ev, int cap, unsigned int *nev, int *error)
+{
+    const uint32_t sh = (uint32_t)(bin & 1) << 4;
+    const uint32_t old = atomicAdd(&words[bin >> 1], 1u << sh);
+    if (__builtin_expect(((old >> sh) & 0xffffu) == 0xffffu, 0)) log_wrap(bin, sh, old, ev, cap, nev, error);
+}
+
+__device__ __forceinline__ double clnc_of(const double *table, unsigned long long c)
+{
+    if (c < 65536ull) return __ldg(table + c);
+    const double x = (double)c;
+    return x * log(x);
+}
+
+template <int MODE>
+__device__ __forceinline__ void bucket_pair(const Binner &b, float va, float vb, int &ka, int &kb)
+{
+    if (MODE == 0) {
+        fast_bucket_pair(b, va, vb, ka, kb);
+    } else {
+        ka = b.mode == 2 ? 0 : exact_bucket(b, va);
+        kb = b.mode == 2 ? 0 : exact_bucket(b, vb);
+    }
+}
+
+template <int MODE>
+__device__ __forceinline__ void stream_pair(const Binner &bn, const float *f1, const float *f2, int64_t n,
+                                            uint32_t *words, int4 *ev, int cap, unsigned int *nev, int *error)
+{
+    const float4 *v1 = reinterpret_cast<const float4 *>(f1);
+    const float4 *v2 = reinterpret_cast<const float4 *>(f2);
+    const int64_t n4 = n >> 2;
+    const int bins = bn.bins;
+    int64_t q = threadIdx.x;
+    float4 x = make_float4(0.f, 0.f, 0.f, 0.f), y = x;
+    if (q < n4) {
+        x = __ldg(v1 + q);
+        y = __ldg(v2 + q);
+    }
+    while (q < n4) {
+        const int64_t qn = q + blockDim.x;
+        float4 xn = x, yn = y;
+        if (qn < n4) {
+            xn = __ldg(v1 + qn);
+            yn = __ldg(v2 + qn);
         }
+        int a0, b0, a1, b1, a2, b2, a3, b3;
+        bucket_pair<MODE>(bn, x.x, y.x, a0, b0);
+        bucket_pair<MODE>(bn, x.y, y.y, a1, b1);
+        bucket_pair<MODE>(bn, x.z, y.z, a2, b2);
+        bucket_pair<MODE>(bn, x.w, y.w, a3, b3);
+        count_bin(words, a0 * bins + b0, ev, cap, nev, error);
+        count_bin(words, a1 * bins + b1, ev, cap, nev, error);
+        count_bin(words, a2 * bins + b2, ev, cap, nev, error);
+        count_bin(words, a3 * bins + b3, ev, cap, nev, error);
+        x = xn;
+        y = yn;
+        q = qn;
+    }
+    for (int64_t v = (n4 << 2) + threadIdx.x; v < n; v += blockDim.x) {
+        int ka, kb;
+        bucket_pair<MODE>(bn, f1[v], f2[v], ka, kb);
+        count_bin(words, ka * bins + kb, ev, cap, nev, error);
     }
 }
 
 __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(PairArgs a)
 {
-    extern __shared__ uint32_t hist_words[];
+    extern __shared__ uint32_t words[];
     __shared__ int s_task;
+    __shared__ unsigned int s_nev;
     __shared__ double s_red[3][HIST_THREADS / 32];
     __shared__ unsigned long long s_colsum[ISO_MAX_BINS];
+    __shared__ unsigned long long s_rowsum[ISO_MAX_BINS];
 
     const int bins = a.bins;
-    const int words = bins * bins / 2;
-    uint32_t *ghist = a.scratch + (size_t)blockIdx.x * bins * bins;
+    const int nwords = bins * bins / 2;
+    const int wpr = bins / 2;  // words per histogram row
+    int4 *ev = a.events + (size_t)blockIdx.x * a.event_cap;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
 
-    for (int w = threadIdx.x; w < words; w += blockDim.x) hist_words[w] = 0;
+    for (int w = threadIdx.x; w < nwords; w += blockDim.x) words[w] = 0;
 
     for (;;) {
-        if (threadIdx.x == 0) s_task = (int)atomicAdd(a.counter, 1u);
+        if (threadIdx.x == 0) {
+            s_task = (int)atomicAdd(a.counter, 1u);
+            s_nev = 0;
+        }
+        for (int c = threadIdx.x; c < bins; c += blockDim.x) {
+            s_colsum[c] = 0;
+            s_rowsum[c] = 0;
+        }
         __syncthreads();
         const int t = s_task;
         if (t >= a.num_tasks) break;
         const int2 task = a.tasks[t];
         const int i = task.x, j = task.y;
 
-        float mn_i = bits_to_float(a.mma[2 * i]), mx_i = bits_to_float(a.mma[2 * i + 1]);
-        float mn_j = bits_to_float(a.mmb[2 * j]), mx_j = bits_to_float(a.mmb[2 * j + 1]);
-        const float mn = mn_i < mn_j ? mn_i : mn_j;
-        const float mx = mx_i > mx_j ? mx_i : mx_j;
-        const float step = __fdiv_rn(__fsub_rn(mx, mn), (float)bins);
+        Binner bn;
+        {
+            const float mn_i = bits_to_float(a.mma[2 * i]), mx_i = bits_to_float(a.mma[2 * i + 1]);
+            const float mn_j = bits_to_float(a.mmb[2 * j]), mx_j = bits_to_float(a.mmb[2 * j + 1]);
+            bn.mn = mn_i < mn_j ? mn_i : mn_j;
+            const float mx = mx_i > mx_j ? mx_i : mx_j;
+            bn.step = __fdiv_rn(__fsub_rn(mx, bn.mn), (float)bins);
+            bn.bins = bins;
+            bn.r = __frcp_rn(bn.step);
+            bn.mode = bn.step == 0.0f ? 2 : (isfinite(bn.r) && bn.step >= 1.17549435e-38f ? 0 : 1);
+        }
 
         const float *f1 = a.fa + (size_t)i * a.stride;
         const float *f2 = a.fb + (size_t)j * a.stride;
@@ -99,95 +235,116 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
         const float4 *v2 = reinterpret_cast<const float4 *>(f2);
         const int64_t n4 = a.n >> 2;
 
-        // block-uniform chunks of at most 63488 voxels: no 16-bit half overflows
-        const int64_t chunk = (int64_t)HIST_ITERS_PER_FLUSH * blockDim.x;
-        for (int64_t base = 0; base < n4; base += chunk) {
-            const int64_t end = base + chunk < n4 ? base + chunk : n4;
-            for (int64_t q = base + threadIdx.x; q < end; q += blockDim.x) {
-                float4 x = __ldg(v1 + q);
-                float4 y = __ldg(v2 + q);
-                count_bin(hist_words, iso_bucket(x.x, mn, step, bins) * bins + iso_bucket(y.x, mn, step, bins));
-                count_bin(hist_words, iso_bucket(x.y, mn, step, bins) * bins + iso_bucket(y.y, mn, step, bins));
-                count_bin(hist_words, iso_bucket(x.z, mn, step, bins) * bins + iso_bucket(y.z, mn, step, bins));
-                count_bin(hist_words, iso_bucket(x.w, mn, step, bins) * bins + iso_bucket(y.w, mn, step, bins));
-            }
-            __syncthreads();
-            flush_packed(hist_words, words, ghist);
-            __syncthreads();
-        }
-        // tail (n not a multiple of 4)
-        for (int64_t v = (n4 << 2) + threadIdx.x; v < a.n; v += blockDim.x)
-            count_bin(hist_words, iso_bucket(f1[v], mn, step, bins) * bins + iso_bucket(f2[v], mn, step, bins));
-        __syncthreads();
-        flush_packed(hist_words, words, ghist);
+        // streaming loop, one load pair in flight ahead of the one being binned
+        if (bn.mode == 0) stream_pair<0>(bn, f1, f2, a.n, words, ev, a.event_cap, &s_nev, a.error);
+        else stream_pair<1>(bn, f1, f2, a.n, words, ev, a.event_cap, &s_nev, a.error);
         __syncthreads();
 
-        // ---- reduction: row sums, column sums, sum c ln c; clears ghist ----
-        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-        for (int c = threadIdx.x; c < bins; c += blockDim.x) s_colsum[c] = 0;
-        __syncthreads();
-        double hxy = 0.0, hy = 0.0;
-        unsigned long long colpart[ISO_MAX_BINS / 32];
-#pragma unroll
-        for (int k = 0; k < ISO_MAX_BINS / 32; ++k) colpart[k] = 0;
-        const bool dump = a.joint_dump != nullptr;
-        const bool dumpcr = a.colrow_dump != nullptr;
-        for (int r = warp; r < bins; r += nwarps) {
-            unsigned long long rowsum = 0;
-            uint32_t *row = ghist + (size_t)r * bins;
-#pragma unroll
-            for (int k = 0; k < ISO_MAX_BINS / 32; ++k) {
-                int c = lane + 32 * k;
-                if (c < bins) {
-                    uint32_t cnt = row[c];
-                    row[c] = 0;
-                    if (dump) {
-                        a.joint_dump[(((size_t)i * a.m + j) * bins + r) * bins + c] = cnt;
-                        if (a.symmetric && i != j) a.joint_dump[(((size_t)j * a.m + i) * bins + c) * bins + r] = cnt;
-                    }
-                    rowsum += cnt;
-                    colpart[k] += cnt;
-                    if (cnt) hxy -= (double)cnt * log((double)cnt);
+        // ---- wrap corrections: per distinct bin, total correction and its
+        // effect on sum(c ln c) and the marginals (events are rare: at most
+        // about 2n/65536 per pair)
+        const int nev = (int)(s_nev < (unsigned int)a.event_cap ? s_nev : (unsigned int)a.event_cap);
+        double hxy = 0.0;
+        for (int e = threadIdx.x; e < nev; e += blockDim.x) {
+            const int bin = ev[e].x;
+            bool first = true;
+            long long corr = 0;
+            for (int g = 0; g < nev; ++g) {
+                if (ev[g].x != bin) continue;
+                if (g < e) {
+                    first = false;
+                    break;
                 }
+                corr += ev[g].y;
             }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) rowsum += __shfl_xor_sync(0xffffffffu, rowsum, o);
-            if (lane == 0 && rowsum) hy -= (double)rowsum * log((double)rowsum);
-            if (lane == 0 && dumpcr) {
-                size_t base = ((size_t)i * a.m + j) * bins;
-                a.colrow_dump[(size_t)a.m * a.m * bins + base + r] = (uint32_t)rowsum;  // row sums of (i,j)
-                if (a.symmetric && i != j) a.colrow_dump[((size_t)j * a.m + i) * bins + r] = (uint32_t)rowsum;  // col sums of (j,i)
+            if (!first) continue;
+            const uint32_t c16 = (words[bin >> 1] >> ((bin & 1) << 4)) & 0xffffu;
+            const unsigned long long ctrue = (unsigned long long)((long long)c16 + corr);
+            hxy -= clnc_of(a.clnc, ctrue) - clnc_of(a.clnc, c16);
+            atomicAdd(&s_rowsum[bin / bins], (unsigned long long)corr);
+            atomicAdd(&s_colsum[bin % bins], (unsigned long long)corr);
+            ev[e].z = (int)c16;
+            ev[e].w = (int)ctrue;  // only read back for histogram dumps
+        }
+        __syncthreads();  // the bin pass below clears the words read above
+
+        // ---- bin pass: 16-bit counts, marginals, sum(c ln c); clears the bins.
+        // Thread (g, w) reads word column w of rows g, g+groups, ...
+        const bool dump = a.joint_dump != nullptr;
+        {
+            const int groups = blockDim.x / wpr;
+            const int w = threadIdx.x % wpr, g = threadIdx.x / wpr;
+            if (g < groups) {
+                uint32_t cs0 = 0, cs1 = 0;
+                for (int r = g; r < bins; r += groups) {
+                    const uint32_t word = words[r * wpr + w];
+                    if (!word && !dump) continue;
+                    words[r * wpr + w] = 0;
+                    const uint32_t c0 = word & 0xffffu, c1 = word >> 16;
+                    cs0 += c0;
+                    cs1 += c1;
+                    atomicAdd(&s_rowsum[r], (unsigned long long)(c0 + c1));
+                    if (c0) hxy -= __ldg(a.clnc + c0);
+                    if (c1) hxy -= __ldg(a.clnc + c1);
+                    if (dump) {
+                        const int c = 2 * w;
+                        a.joint_dump[(((size_t)i * a.m + j) * bins + r) * bins + c] = c0;
+                        a.joint_dump[(((size_t)i * a.m + j) * bins + r) * bins + c + 1] = c1;
+                        if (a.symmetric && i != j) {
+                            a.joint_dump[(((size_t)j * a.m + i) * bins + c) * bins + r] = c0;
+                            a.joint_dump[(((size_t)j * a.m + i) * bins + c + 1) * bins + r] = c1;
+                        }
+                    }
+                }
+                if (cs0) atomicAdd(&s_colsum[2 * w], (unsigned long long)cs0);
+                if (cs1) atomicAdd(&s_colsum[2 * w + 1], (unsigned long long)cs1);
             }
         }
-#pragma unroll
-        for (int k = 0; k < ISO_MAX_BINS / 32; ++k) {
-            int c = lane + 32 * k;
-            if (c < bins && colpart[k]) atomicAdd(&s_colsum[c], colpart[k]);
+        __syncthreads();
+        if (dump && nev > 0) {
+            // overwrite the corrected bins (distinct events carry c16 != or corr)
+            for (int e = threadIdx.x; e < nev; e += blockDim.x) {
+                const int bin = ev[e].x;
+                bool first = true;
+                for (int g = 0; g < e; ++g)
+                    if (ev[g].x == bin) {
+                        first = false;
+                        break;
+                    }
+                if (!first) continue;
+                const int r = bin / bins, c = bin % bins;
+                const uint32_t val = (uint32_t)ev[e].w;
+                a.joint_dump[(((size_t)i * a.m + j) * bins + r) * bins + c] = val;
+                if (a.symmetric && i != j) a.joint_dump[(((size_t)j * a.m + i) * bins + c) * bins + r] = val;
+            }
+        }
+        double hx = 0.0, hy = 0.0;
+        for (int c = threadIdx.x; c < bins; c += blockDim.x) {
+            const unsigned long long cs = s_colsum[c], rs = s_rowsum[c];
+            if (cs) hx -= clnc_of(a.clnc, cs);
+            if (rs) hy -= clnc_of(a.clnc, rs);
+            if (a.colrow_dump) {
+                const size_t mm = (size_t)a.m * a.m * bins;
+                const size_t bij = ((size_t)i * a.m + j) * bins, bji = ((size_t)j * a.m + i) * bins;
+                a.colrow_dump[bij + c] = (uint32_t)cs;        // column sums of (i,j)
+                a.colrow_dump[mm + bij + c] = (uint32_t)rs;   // row sums of (i,j)
+                if (a.symmetric && i != j) {
+                    a.colrow_dump[bji + c] = (uint32_t)rs;
+                    a.colrow_dump[mm + bji + c] = (uint32_t)cs;
+                }
+            }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             hxy += __shfl_xor_sync(0xffffffffu, hxy, o);
+            hx += __shfl_xor_sync(0xffffffffu, hx, o);
             hy += __shfl_xor_sync(0xffffffffu, hy, o);
         }
         if (lane == 0) {
             s_red[0][warp] = hxy;
             s_red[1][warp] = hy;
+            s_red[2][warp] = hx;
         }
-        __syncthreads();
-        double hx = 0.0;
-        for (int c = threadIdx.x; c < bins; c += blockDim.x) {
-            unsigned long long cs = s_colsum[c];
-            if (cs) hx -= (double)cs * log((double)cs);
-            if (dumpcr) {
-                size_t base = ((size_t)i * a.m + j) * bins;
-                a.colrow_dump[base + c] = (uint32_t)cs;  // col sums of (i,j)
-                if (a.symmetric && i != j)
-                    a.colrow_dump[(size_t)a.m * a.m * bins + ((size_t)j * a.m + i) * bins + c] = (uint32_t)cs;  // row sums of (j,i)
-            }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) hx += __shfl_xor_sync(0xffffffffu, hx, o);
-        if (lane == 0) s_red[2][warp] = hx;
         __syncthreads();
         if (threadIdx.x == 0) {
             double sxy = 0.0, sy = 0.0, sx = 0.0;
@@ -201,14 +358,20 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
             sxy = sxy / N + lnN;
             sx = sx / N + lnN;
             sy = sy / N + lnN;
-            double iXY = sx + sy - sxy;
-            double val = 2.0 * iXY / (sx + sy);
-            float out = val != val ? 0.0f : (float)val;
+            const double iXY = sx + sy - sxy;
+            const double val = 2.0 * iXY / (sx + sy);
+            const float out = val != val ? 0.0f : (float)val;
             a.ism[(size_t)i * a.m + j] = out;
             if (a.symmetric) a.ism[(size_t)j * a.m + i] = out;
         }
         __syncthreads();
     }
+}
+
+__global__ void clnc_table_kernel(double *table)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < 65536) table[c] = c < 2 ? 0.0 : (double)c * log((double)c);
 }
 
 // Per-field min/max over the first n values: min starts at FLT_MAX and max at
@@ -291,11 +454,18 @@ int iso_run_similarity(iso_ctx *ctx, const float *d_fields_a, const float *d_fie
     int num_tasks = 0;
     build_tasks(m, symmetric, h_tasks.data(), &num_tasks);
 
-    void *d_tasks = nullptr, *d_counter = nullptr, *d_scratch = nullptr;
+    void *d_tasks = nullptr, *d_counter = nullptr, *d_events = nullptr, *d_clnc = nullptr;
     ISO_TRY(iso_buf(ctx, BUF_PAIR_TASKS, max_tasks * sizeof(int2), &d_tasks));
     ISO_TRY(iso_buf(ctx, BUF_TASK_COUNTER, 256, &d_counter));
     ISO_CUDA(cudaMemcpyAsync(d_tasks, h_tasks.data(), num_tasks * sizeof(int2), cudaMemcpyHostToDevice, ctx->stream));
-    ISO_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned int), ctx->stream));
+    ISO_CUDA(cudaMemsetAsync(d_counter, 0, 2 * sizeof(unsigned int), ctx->stream));
+    if (!ctx->clnc_ready) {
+        ISO_TRY(iso_buf(ctx, BUF_CLNC, 65536 * sizeof(double), &d_clnc));
+        clnc_table_kernel<<<256, 256, 0, ctx->stream>>>((double *)d_clnc);
+        ISO_LAUNCHED(ctx);
+        ctx->clnc_ready = true;
+    }
+    d_clnc = ctx->buf[BUF_CLNC];
 
     const size_t smem = (size_t)bins * bins / 2 * sizeof(uint32_t);
     ISO_CUDA(cudaFuncSetAttribute(joint_histogram_mi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -305,9 +475,10 @@ int iso_run_similarity(iso_ctx *ctx, const float *d_fields_a, const float *d_fie
     if (per_sm < 1) per_sm = 1;
     int grid = ctx->num_sms * per_sm;
     if (grid > num_tasks) grid = num_tasks;
-    ISO_TRY(iso_buf(ctx, BUF_HIST_SCRATCH, (size_t)grid * bins * bins * sizeof(uint32_t), &d_scratch));
-    // scratch must start zero; the kernel leaves it zero after every task
-    ISO_CUDA(cudaMemsetAsync(d_scratch, 0, (size_t)grid * bins * bins * sizeof(uint32_t), ctx->stream));
+    // wrap events per pair: each needs 65536 increments of one 16-bit half
+    const int64_t event_cap = 2 * (n / 65536 + 1) + 64;
+    if (event_cap > 0x7fffffff / 2) return iso_fail(ISO_ERR_ARG, "fields too long (%lld values)", (long long)n);
+    ISO_TRY(iso_buf(ctx, BUF_HIST_SCRATCH, (size_t)grid * event_cap * sizeof(int4), &d_events));
 
     PairArgs a;
     a.fa = d_fields_a;
@@ -322,11 +493,18 @@ int iso_run_similarity(iso_ctx *ctx, const float *d_fields_a, const float *d_fie
     a.bins = bins;
     a.symmetric = symmetric ? 1 : 0;
     a.ism = d_ism;
-    a.scratch = (uint32_t *)d_scratch;
+    a.events = (int4 *)d_events;
+    a.event_cap = (int)event_cap;
+    a.clnc = (const double *)d_clnc;
     a.counter = (unsigned int *)d_counter;
+    a.error = (int *)d_counter + 1;
     a.joint_dump = d_joint_dump;
     a.colrow_dump = d_colrow_dump;
     joint_histogram_mi_kernel<<<grid, HIST_THREADS, smem, ctx->stream>>>(a);
     ISO_LAUNCHED(ctx);
+    int err = 0;
+    ISO_CUDA(cudaMemcpyAsync(&err, a.error, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    ISO_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (err) return iso_fail(ISO_ERR_INTERNAL, "joint histogram: wrap-event list overflow (code %d)", err);
     return ISO_OK;
 }

@@ -75,6 +75,7 @@ enum IsoBuf {
     BUF_CUB_TEMP,
     BUF_STAGING_A,
     BUF_STAGING_B,
+    BUF_CLNC,            // c*ln(c) for c < 65536, FP64
     BUF_COUNT_
 };
 
@@ -87,6 +88,7 @@ struct iso_ctx {
     int64_t launches = 0;
     void *host_pinned = nullptr;
     size_t host_pinned_cap = 0;
+    bool clnc_ready = false;
 };
 
 // Ensures buffer `b` holds at least `bytes`; contents are not preserved.

@@ -94,3 +94,44 @@ def test_deterministic(ctx):
     a = ctx.similarity_map(f, 256)
     b = ctx.similarity_map(f, 256)
     assert np.array_equal(a, b)
+
+
+def test_bucket_boundaries_bit_exact(ctx):
+    """Values exactly on bucket boundaries (min + k*step) and one ulp either
+    side: the reciprocal fast path must hand every near-boundary value to the
+    exact division."""
+    bins = 256
+    mn, mx = np.float32(0.0), np.float32(1.7)
+    step = np.float32(mx - mn) / np.float32(bins)
+    ks = np.arange(bins + 1, dtype=np.float32)
+    on = (ks * step).astype(np.float32)
+    vals = np.concatenate([on, np.nextafter(on, np.float32(-1)), np.nextafter(on, np.float32(9)),
+                           [mn, mx]]).astype(np.float32)
+    vals = np.clip(vals, mn, mx)
+    rng = np.random.default_rng(2)
+    n = 4 * len(vals)
+    f1 = np.resize(vals, n).astype(np.float32)
+    f2 = rng.permutation(f1).astype(np.float32)
+    f = np.stack([f1, f2])
+    _, joint = ctx.similarity_map(f, bins, joint=True)
+    for i in range(2):
+        for j in range(2):
+            want, _, _ = oracle.pair_histogram(f[i], f[j], bins)
+            assert np.array_equal(joint[i, j], want)
+
+
+@pytest.mark.parametrize("bins", [2, 4])
+def test_counter_wraps(ctx, bins):
+    """More than 65536 hits per bin in both halves of a packed counter word:
+    the wrap corrections must restore the exact counts."""
+    rng = np.random.default_rng(bins)
+    n = 1_000_003
+    f = rng.integers(0, bins, size=(3, n)).astype(np.float32)
+    f[:, 0] = 0
+    f[:, 1] = bins - 1
+    ism, joint = ctx.similarity_map(f, bins, joint=True)
+    for i in range(3):
+        for j in range(3):
+            want, _, _ = oracle.pair_histogram(f[i], f[j], bins)
+            assert np.array_equal(joint[i, j], want), (i, j)
+    assert np.abs(ism - oracle.similarity_map(f, bins, mode=0)).max() < TOL_F64

@@ -86,14 +86,30 @@ def test_approximation_golden_and_random(ctx):
 
 def test_reference_named_surface_entries():
     import isosim
-    dims = (16, 14, 12)
+    dims = (32, 30, 28)
     vol = blobs(dims, 3)
     iso = float(np.float32((vol.min() + vol.max()) / 2))
     cells = isosim.approximate_isosurfaces_h(vol.ravel(), dims, iso)
     assert np.array_equal(cells, oracle.approximation(vol, dims, iso))
     v4 = isosim.marching_cube_h(vol.ravel(), dims, iso)
-    want, _, _ = oracle.marching_cubes(vol, dims, iso, frame=0)
+    want, _, total = oracle.marching_cubes(vol, dims, iso, frame=0)
+    assert total <= dims[0] * dims[1] * dims[2] - 3
     assert np.array_equal(v4[:, :3], want) and np.all(v4[:, 3] == 1.0)
+
+
+def test_marching_cube_entry_reports_reference_truncation():
+    """Beyond maxVerts-3 triangle vertices the reference drops triangles and
+    lets unwritten slots into its vertex set; the C entry refuses instead."""
+    import isosim
+    dims = (10, 10, 10)
+    vol = np.random.default_rng(8).standard_normal(dims).astype(np.float32)
+    _, _, total = oracle.marching_cubes(vol, dims, 0.0, frame=0)
+    assert total > 1000 - 3
+    with pytest.raises(isosim.IsoError) as e:
+        isosim.marching_cube_h(vol.ravel(), dims, 0.0)
+    assert e.value.code == isosim.ISO_ERR_CAPACITY
+    pts, stats = isosim.Context(0).surface_points(vol.ravel(), dims, [0.0])
+    assert stats[0].flags & isosim.MC_REF_DROPPED
 
 
 def test_empty_and_out_of_range(ctx):
