@@ -218,6 +218,32 @@ ISO_API int iso_marching_cube_h(float iso, int dimX, int dimY, int dimZ, const f
 ISO_API int iso_generate_hierarchy_h(const float *points_xyz, long numPoints, int dimX, int dimY, int dimZ,
                                      float *h_distances, int numSamples, int dfDownscale);
 
+/* ---------------------------------------------------------------------- */
+/* Allocation-free similarity map (no counterpart in the reference)        */
+/* ---------------------------------------------------------------------- */
+
+#define ISO_NOALLOC_MAX_FIELDS 256
+#define ISO_NOALLOC_MAX_VALUES 16777216
+
+/* The same similarity map as iso_similarity_map, for callers that must not
+ * allocate GPU memory during the call: a process running under a fixed,
+ * pre-committed device-memory budget, or code on a path where a call into the
+ * allocator could block or fail.  Nothing is allocated: all scratch is a
+ * fixed array of about 3.2 MB inside this library, which every device that
+ * loads the library keeps until the process exits.
+ *   d_fields: m rows of n float32 values in device memory, row i at
+ *             d_fields + i*stride (16-byte aligned base, stride >= n and a
+ *             multiple of 4);  d_ism_out: m*m floats of device memory;
+ *   stream:   a cudaStream_t (NULL = legacy default stream); the call
+ *             synchronises it before returning.
+ * Limits: m <= ISO_NOALLOC_MAX_FIELDS, n <= ISO_NOALLOC_MAX_VALUES, bins even
+ * in [2, 256]; larger sizes return ISO_ERR_CAPACITY.  The first call on a
+ * device looks up the array's device address and fills a lookup table, so
+ * make it before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race. */
+ISO_API int iso_similarity_map_noalloc(const float *d_fields, int m, int64_t n, int64_t stride, int bins,
+                                       float *d_ism_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -16,6 +16,7 @@
 // the CTA reduces that histogram: FP64 sum of c*ln(c) over bins and over the
 // exact integer row and column sums, then NMI = 2I/(hX+hY), written to both
 // (i,j) and (j,i).
+#include <mutex>
 #include <vector>
 
 #include "iso_internal.cuh"
@@ -506,5 +507,164 @@ int iso_run_similarity(iso_ctx *ctx, const float *d_fields_a, const float *d_fie
     ISO_CUDA(cudaMemcpyAsync(&err, a.error, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     ISO_CUDA(cudaStreamSynchronize(ctx->stream));
     if (err) return iso_fail(ISO_ERR_INTERNAL, "joint histogram: wrap-event list overflow (code %d)", err);
+    return ISO_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free similarity map
+//
+// For callers that must not allocate device memory while they run, for
+// example a host process that hands the GPU a fixed memory budget up front,
+// or code that runs where allocating would stall or fail (an allocator
+// callback, a tight service loop that must not touch the driver's allocator).
+// All scratch lives in one file-scope device array of fixed size, loaded with
+// this library and kept by every device until the process exits.  The
+// caller's fields and output are device memory the caller owns.
+//
+// Limits: at most ISO_NOALLOC_MAX_FIELDS fields of at most
+// ISO_NOALLOC_MAX_VALUES values each, 2..256 bins (even).
+//
+// The first call on a device resolves the array's device address with
+// cudaGetSymbolAddress (with that device current) and fills the c*ln(c)
+// table; make that first call before any stream capture.  Every call reuses
+// the same array: calls that overlap on the GPU (different streams, or
+// concurrent host threads on one device) race and corrupt each other.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr int NOALLOC_MAX_CTAS = 256;
+constexpr int64_t NOALLOC_EVENT_CAP = 2 * (ISO_NOALLOC_MAX_VALUES / 65536 + 1) + 64;
+constexpr size_t NA_OFF_CLNC = 0;
+constexpr size_t NA_OFF_TASKS = NA_OFF_CLNC + 65536 * sizeof(double);
+constexpr size_t NA_MAX_TASKS = (size_t)ISO_NOALLOC_MAX_FIELDS * (ISO_NOALLOC_MAX_FIELDS + 1) / 2;
+constexpr size_t NA_OFF_MINMAX = (NA_OFF_TASKS + NA_MAX_TASKS * sizeof(int2) + 255) / 256 * 256;
+constexpr size_t NA_OFF_CTRL = NA_OFF_MINMAX + (2 * ISO_NOALLOC_MAX_FIELDS * sizeof(uint32_t) + 255) / 256 * 256;
+constexpr size_t NA_OFF_EVENTS = NA_OFF_CTRL + 256;
+constexpr size_t NA_BYTES = NA_OFF_EVENTS + (size_t)NOALLOC_MAX_CTAS * NOALLOC_EVENT_CAP * sizeof(int4);
+
+// The scratch array (about 3.2 MB).  Host code may not use this name as an
+// address: it refers to a host-side stand-in; the device address comes from
+// cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+struct NoAllocDevice {
+    unsigned char *scratch = nullptr;  // device address of g_noalloc_scratch
+    int grid = 0;
+};
+NoAllocDevice g_noalloc_dev[NOALLOC_MAX_DEVICES];
+std::mutex g_noalloc_mu;
+
+// Upper-triangle pair list, row-major (i <= j).
+__global__ void noalloc_tasks_kernel(int2 *tasks, int m)
+{
+    const int i = blockIdx.x;
+    for (int j = i + threadIdx.x; j < m; j += blockDim.x) {
+        const int64_t idx = (int64_t)i * m - (int64_t)i * (i - 1) / 2 + (j - i);
+        tasks[idx] = make_int2(i, j);
+    }
+}
+
+int noalloc_setup(int device, NoAllocDevice **out)
+{
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    NoAllocDevice &d = g_noalloc_dev[device];
+    if (!d.scratch) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return iso_fail(ISO_ERR_CUDA, "iso_similarity_map_noalloc: cudaGetSymbolAddress failed: %s",
+                            cudaGetErrorString(e));
+        ISO_CUDA(cudaFuncSetAttribute(joint_histogram_mi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(ISO_MAX_BINS * ISO_MAX_BINS / 2 * sizeof(uint32_t))));
+        int sms = 0, per_sm = 0;
+        ISO_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        ISO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, joint_histogram_mi_kernel, HIST_THREADS,
+                                                               ISO_MAX_BINS * ISO_MAX_BINS / 2 * sizeof(uint32_t)));
+        int grid = sms * (per_sm < 1 ? 1 : per_sm);
+        d.grid = grid < NOALLOC_MAX_CTAS ? grid : NOALLOC_MAX_CTAS;
+        clnc_table_kernel<<<256, 256>>>((double *)((unsigned char *)p + NA_OFF_CLNC));
+        ISO_CUDA(cudaGetLastError());
+        ISO_CUDA(cudaDeviceSynchronize());
+        d.scratch = (unsigned char *)p;
+    }
+    *out = &d;
+    return ISO_OK;
+}
+
+}  // namespace
+
+extern "C" int iso_similarity_map_noalloc(const float *d_fields, int m, int64_t n, int64_t stride, int bins,
+                                          float *d_ism_out, void *stream)
+{
+    iso_clear_error();
+    if (!d_fields || !d_ism_out) return iso_fail(ISO_ERR_ARG, "iso_similarity_map_noalloc: NULL pointer");
+    if (m < 1 || m > ISO_NOALLOC_MAX_FIELDS)
+        return iso_fail(ISO_ERR_CAPACITY, "iso_similarity_map_noalloc: %d fields; the limit is %d", m,
+                        ISO_NOALLOC_MAX_FIELDS);
+    if (n < 1 || n > ISO_NOALLOC_MAX_VALUES)
+        return iso_fail(ISO_ERR_CAPACITY, "iso_similarity_map_noalloc: %lld values per field; the limit is %d",
+                        (long long)n, ISO_NOALLOC_MAX_VALUES);
+    if (bins < 2 || bins > ISO_MAX_BINS || (bins & 1))
+        return iso_fail(ISO_ERR_ARG, "iso_similarity_map_noalloc: bins must be even and in [2, %d]", ISO_MAX_BINS);
+    if (stride < n || stride % 4 != 0 || ((uintptr_t)d_fields & 15))
+        return iso_fail(ISO_ERR_ARG,
+                        "iso_similarity_map_noalloc: rows need a 16-byte aligned base and a stride >= n, multiple of 4");
+    if (!iso_is_device_ptr(d_fields) || !iso_is_device_ptr(d_ism_out))
+        return iso_fail(ISO_ERR_ARG, "iso_similarity_map_noalloc: fields and output must be device memory");
+    int device = 0;
+    ISO_CUDA(cudaGetDevice(&device));
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES)
+        return iso_fail(ISO_ERR_ARG, "iso_similarity_map_noalloc: device %d out of range", device);
+    NoAllocDevice *d = nullptr;
+    ISO_TRY(noalloc_setup(device, &d));
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned char *base = d->scratch;
+    int2 *tasks = (int2 *)(base + NA_OFF_TASKS);
+    uint32_t *minmax = (uint32_t *)(base + NA_OFF_MINMAX);
+    unsigned int *ctrl = (unsigned int *)(base + NA_OFF_CTRL);
+    const int num_tasks = (int)((int64_t)m * (m + 1) / 2);
+
+    // the counter and error word must start at zero; the rest is overwritten
+    ISO_CUDA(cudaMemsetAsync(ctrl, 0, 2 * sizeof(unsigned int), st));
+    noalloc_tasks_kernel<<<m, 256, 0, st>>>(tasks, m);
+    ISO_CUDA(cudaGetLastError());
+    minmax_init_kernel<<<(m + 255) / 256, 256, 0, st>>>(minmax, m);
+    ISO_CUDA(cudaGetLastError());
+    {
+        const int64_t per = (n + 255) / 256;
+        const int bx = (int)(per < 64 ? (per < 1 ? 1 : per) : 64);
+        field_minmax_kernel<<<dim3(bx, m), 256, 0, st>>>(d_fields, n, stride, minmax);
+        ISO_CUDA(cudaGetLastError());
+    }
+    PairArgs a;
+    a.fa = d_fields;
+    a.fb = d_fields;
+    a.n = n;
+    a.stride = stride;
+    a.mma = minmax;
+    a.mmb = minmax;
+    a.tasks = tasks;
+    a.num_tasks = num_tasks;
+    a.m = m;
+    a.bins = bins;
+    a.symmetric = 1;
+    a.ism = d_ism_out;
+    a.events = (int4 *)(base + NA_OFF_EVENTS);
+    a.event_cap = (int)NOALLOC_EVENT_CAP;
+    a.clnc = (const double *)(base + NA_OFF_CLNC);
+    a.counter = ctrl;
+    a.error = (int *)(ctrl + 1);
+    a.joint_dump = nullptr;
+    a.colrow_dump = nullptr;
+    const int grid = d->grid < num_tasks ? d->grid : num_tasks;
+    const size_t smem = (size_t)bins * bins / 2 * sizeof(uint32_t);
+    joint_histogram_mi_kernel<<<grid, HIST_THREADS, smem, st>>>(a);
+    ISO_CUDA(cudaGetLastError());
+    int err = 0;
+    ISO_CUDA(cudaMemcpyAsync(&err, ctrl + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ISO_CUDA(cudaStreamSynchronize(st));
+    if (err) return iso_fail(ISO_ERR_INTERNAL, "iso_similarity_map_noalloc: wrap-event list overflow (code %d)", err);
     return ISO_OK;
 }
