@@ -177,6 +177,18 @@ ISO_API int iso_isovalues(iso_ctx *ctx, const float *volume, int64_t V, float vm
 ISO_API int iso_real_range(iso_ctx *ctx, const float *volume, int64_t V, float cfg_min, float cfg_max,
                            float *out_min, float *out_max);
 
+/* Reorders a volume stored x-fastest (the .dat file layout read by
+ * filehandler/src/BinaryFloatReader.cpp:29-48, element x + y*X + z*X*Y) into
+ * the img order (z fastest, x*Y*Z + y*Z + z) on the GPU.  src and dst: host or
+ * device, X*Y*Z floats each. */
+ISO_API int iso_transpose_xfastest(iso_ctx *ctx, const float *src, int X, int Y, int Z, float *dst);
+
+/* Copies row `row` of the distance-field matrix left by the context's last
+ * iso_ism call (row = map index, i.e. field_ids_out[row]'s surface) to `out`
+ * (host or device, (X/ds)(Y/ds)(Z/ds) floats) -- the representative
+ * fields the single module writes as distancefield-<k>.df. */
+ISO_API int iso_copy_field(iso_ctx *ctx, int row, float *out);
+
 /* ---------------------------------------------------------------------- */
 /* Reference-named entry points (drop-in for isosurfaces_cuda/funcs.h)     */
 /* ---------------------------------------------------------------------- */

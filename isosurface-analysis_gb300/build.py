@@ -17,6 +17,9 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_obj")
 LIB = os.path.join(HERE, "lib")
 TARGET = os.path.join(LIB, "libisosim.so")
+HOST = os.path.join(HERE, "host")
+CLI = os.path.join(HERE, "bin", "isosim")
+HOST_SOURCES = ["main.cpp", "modules.cpp"]
 
 SOURCES = [
     "iso_context.cu",
@@ -82,9 +85,26 @@ def build(force=False, verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    build_cli(force)
     if verbose:
-        print("built", TARGET)
+        print("built", TARGET, "and", CLI)
     return TARGET
+
+
+def build_cli(force=False):
+    """The module CLI (host C++ only, linked against libisosim.so)."""
+    os.makedirs(os.path.dirname(CLI), exist_ok=True)
+    srcs = [os.path.join(HOST, s) for s in HOST_SOURCES]
+    deps = srcs + [os.path.join(HOST, h) for h in ("json.hpp", "dao.hpp", "modules.hpp")] + [TARGET]
+    if not force and os.path.exists(CLI) and all(os.path.getmtime(d) <= os.path.getmtime(CLI) for d in deps):
+        return CLI
+    cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-Wall", "-ffp-contract=off",
+           "-I", os.path.join(ROOT, "include"), "-o", CLI] + srcs + \
+          ["-L", LIB, "-lisosim", "-Wl,-rpath,$ORIGIN/../lib", "-lpthread"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("CLI build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return CLI
 
 
 if __name__ == "__main__":

@@ -89,6 +89,9 @@ struct iso_ctx {
     void *host_pinned = nullptr;
     size_t host_pinned_cap = 0;
     bool clnc_ready = false;
+    // shape of the distance-field matrix left by the last iso_ism call
+    int last_m = 0;
+    int64_t last_F = 0, last_stride = 0;
 };
 
 // Ensures buffer `b` holds at least `bytes`; contents are not preserved.

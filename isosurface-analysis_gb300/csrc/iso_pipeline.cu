@@ -93,6 +93,24 @@ __global__ void uniform_hist_kernel(const float *vol, int64_t count, float gmin,
     }
 }
 
+// dst[x*Y*Z + y*Z + z] = src[x + y*X + z*X*Y], through a 32x32 shared tile over
+// the (x, z) plane of each y slice so both sides are coalesced.
+__global__ void transpose_xz_kernel(const float *src, float *dst, int X, int Y, int Z)
+{
+    __shared__ float tile[32][33];
+    const int y = blockIdx.z;
+    const int x0 = blockIdx.x * 32, z0 = blockIdx.y * 32;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int x = x0 + threadIdx.x, z = z0 + k;
+        if (x < X && z < Z) tile[k][threadIdx.x] = src[(size_t)x + (size_t)y * X + (size_t)z * X * Y];
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int z = z0 + threadIdx.x, x = x0 + k;
+        if (x < X && z < Z) dst[(size_t)x * Y * Z + (size_t)y * Z + z] = tile[threadIdx.x][k];
+    }
+}
+
 void sort_points_host(std::vector<float> &xyz)
 {
     const size_t n = xyz.size() / 3;
@@ -173,6 +191,9 @@ extern "C" int iso_ism(iso_ctx *ctx, const float *volume, int X, int Y, int Z, c
     ISO_CUDA(cudaStreamSynchronize(ctx->stream));
     ISO_CUDA(cudaMemcpy(field_ids_out, ids.data(), (size_t)m * sizeof(int32_t), cudaMemcpyDefault));
     *m_out = m;
+    ctx->last_m = m;
+    ctx->last_F = F;
+    ctx->last_stride = stride;
     if (stats_out) memcpy(stats_out, stats.data(), (size_t)n * sizeof(iso_surface_stats));
     if (timing_out) {
         cudaEventElapsedTime(&timing_out->surface_ms, ev[0], ev[1]);
@@ -189,6 +210,7 @@ extern "C" int iso_cross_map(iso_ctx *ctx, const float *fields_a, const float *f
     iso_clear_error();
     if (!ctx || !fields_a || !fields_b || !out || m <= 0 || n <= 0) return iso_fail(ISO_ERR_ARG, "iso_cross_map: bad argument");
     ISO_CUDA(cudaSetDevice(ctx->device));
+    ctx->last_m = 0;
     const int64_t stride = round_up(n, 64);
     void *d_fields, *d_mm, *d_ism;
     ISO_TRY(iso_buf(ctx, BUF_FIELDS, (size_t)2 * m * stride * sizeof(float), &d_fields));
@@ -261,6 +283,7 @@ extern "C" int iso_distance_field(iso_ctx *ctx, const float *points, int64_t P, 
     iso_clear_error();
     if (!ctx || !points || !out || P < 1) return iso_fail(ISO_ERR_ARG, "iso_distance_field: bad argument");
     ISO_CUDA(cudaSetDevice(ctx->device));
+    ctx->last_m = 0;
     const int ds = downscale < 1 ? 1 : downscale;
     void *d_xyz, *d_norm;
     ISO_TRY(iso_buf(ctx, BUF_STAGING_A, (size_t)P * 3 * sizeof(float), &d_xyz));
@@ -282,6 +305,7 @@ static int similarity_impl(iso_ctx *ctx, const float *const *field_ptrs, const f
                            uint32_t *joint_out, uint32_t *col_out, uint32_t *row_out, bool multi)
 {
     ISO_CUDA(cudaSetDevice(ctx->device));
+    ctx->last_m = 0;  // the field matrix is reused below
     const int nf = multi ? 2 * m : m;
     const int64_t stride = round_up(n, 64);
     void *d_fields, *d_mm, *d_ism;
@@ -422,6 +446,37 @@ extern "C" int iso_isovalues(iso_ctx *ctx, const float *volume, int64_t V, float
         out[i] = vmin + step * (float)mid;
         last = idx;
     }
+    return ISO_OK;
+}
+
+extern "C" int iso_transpose_xfastest(iso_ctx *ctx, const float *src, int X, int Y, int Z, float *dst)
+{
+    iso_clear_error();
+    if (!ctx || !src || !dst || X < 1 || Y < 1 || Z < 1) return iso_fail(ISO_ERR_ARG, "iso_transpose_xfastest: bad argument");
+    if (Y > 65535) return iso_fail(ISO_ERR_ARG, "iso_transpose_xfastest: Y above 65535");
+    ISO_CUDA(cudaSetDevice(ctx->device));
+    const size_t V = (size_t)X * Y * Z;
+    void *a, *b;
+    ISO_TRY(iso_buf(ctx, BUF_STAGING_A, V * sizeof(float), &a));
+    ISO_TRY(iso_buf(ctx, BUF_STAGING_B, V * sizeof(float), &b));
+    ISO_CUDA(cudaMemcpyAsync(a, src, V * sizeof(float), cudaMemcpyDefault, ctx->stream));
+    dim3 grid((X + 31) / 32, (Z + 31) / 32, Y);
+    transpose_xz_kernel<<<grid, dim3(32, 8), 0, ctx->stream>>>((const float *)a, (float *)b, X, Y, Z);
+    ISO_LAUNCHED(ctx);
+    ISO_CUDA(cudaMemcpyAsync(dst, b, V * sizeof(float), cudaMemcpyDefault, ctx->stream));
+    ISO_CUDA(cudaStreamSynchronize(ctx->stream));
+    return ISO_OK;
+}
+
+extern "C" int iso_copy_field(iso_ctx *ctx, int row, float *out)
+{
+    iso_clear_error();
+    if (!ctx || !out || row < 0 || row >= ctx->last_m)
+        return iso_fail(ISO_ERR_ARG, "iso_copy_field: row %d outside the last map (%d rows)", row, ctx ? ctx->last_m : 0);
+    ISO_CUDA(cudaSetDevice(ctx->device));
+    ISO_CUDA(cudaMemcpyAsync(out, (const float *)ctx->buf[BUF_FIELDS] + (size_t)row * ctx->last_stride,
+                             (size_t)ctx->last_F * sizeof(float), cudaMemcpyDefault, ctx->stream));
+    ISO_CUDA(cudaStreamSynchronize(ctx->stream));
     return ISO_OK;
 }
 

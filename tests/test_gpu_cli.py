@@ -1,0 +1,107 @@
+"""The module CLI end to end on the GPU: single (voxel approximation), script
+(marching cubes) and multi (cross maps), against the engine API and the oracle."""
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CLI = os.path.join(ROOT, "isosurface-analysis_gb300", "bin", "isosim")
+
+
+def write_dat(path, vol):
+    # .dat files are x-fastest: element x + y*X + z*X*Y
+    np.asarray(vol, np.float32).transpose(2, 1, 0).tofile(path)
+
+
+def make_volume(seed, dims=(20, 18, 16)):
+    import isosim.synth as synth
+    return synth.gaussian_blobs(dims, 4, seed, sigma=(2.0, 5.0))
+
+
+def test_single_module(tmp_path):
+    import isosim
+    dims = (20, 18, 16)
+    vol = make_volume(1, dims)
+    write_dat(tmp_path / "vol.dat", vol)
+    cfg = {"fileName": str(tmp_path / "vol"), "dimensions": list(dims), "minValue": -1e9, "maxValue": 1e9,
+           "outputFolder": str(tmp_path / "out"), "variableName": "V", "timestep": 3, "jsonFile": "meta.json",
+           "dfDownscale": 1, "engine": {"isovalues": 24, "bins": 32, "representatives": 5}}
+    (tmp_path / "single.json").write_text(json.dumps(cfg))
+    r = subprocess.run([CLI, "single", str(tmp_path / "single.json")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr + r.stdout
+    lo, hi = oracle.real_range(vol, -1e9, 1e9)
+    isos = oracle.isovalues(vol, lo, hi, 24, uniform=True)
+    with isosim.Context(0) as ctx:
+        ism, ids, _, _ = ctx.ism(vol.ravel(), dims, isos, surface=isosim.SURFACE_APPROX, bins=32)
+    folder = tmp_path / "out" / "V-3"
+    got = np.fromfile(folder / "similarityMap-24--approx-scale_1" / "map.dat", np.float32)
+    assert np.array_equal(got, ism.ravel())
+    reps = isosim.select_representatives(ism, ids, isos, 5)
+    meta = json.loads((tmp_path / "out" / "meta.json").read_text())
+    vol_info = meta["volumes"][0]
+    assert meta["variables"] == ["V"] and vol_info["timestep"] == 3 and vol_info["numIsovalues"] == len(ids)
+    assert [r["valueId"] for r in vol_info["representatives"]] == [r[2] for r in reps]
+    rank = sorted(r[2] for r in reps)
+    for r in reps:
+        df = np.fromfile(folder / "distancefields" / ("distancefield-%d.df" % rank.index(r[2])), np.float32)
+        cells = oracle.approximation(vol, dims, float(isos[r[2]])).astype(np.float32)
+        assert np.array_equal(df, oracle.distance_field_f32(oracle.normalize_points(cells, dims), dims))
+    # a second run skips the processed volume
+    r = subprocess.run([CLI, "single", str(tmp_path / "single.json")], capture_output=True, text=True)
+    assert "already processed" in r.stdout
+    assert len(json.loads((tmp_path / "out" / "meta.json").read_text())["volumes"]) == 1
+
+
+def test_script_then_multi(tmp_path):
+    import isosim
+    dims = (16, 16, 16)
+    variables = ["A", "B"]
+    steps = [0, 1]
+    inp = tmp_path / "in"
+    for v in variables:
+        (inp / v).mkdir(parents=True)
+        for t in steps:
+            write_dat(inp / v / ("%s%04d.dat" % (v, t)), make_volume(10 * len(v) + t + (5 if v == "B" else 0), dims))
+    cfg = {"entries": [{"dimensions": list(dims), "timesteps": steps, "dfDownscale": 1,
+                        "fileFormatString": "%s/%s/%s%04d", "inputFolder": str(inp),
+                        "outputFolder": str(tmp_path / "out"), "jsonFile": "meta.json",
+                        "variables": [{"name": v, "minValue": -1e9, "maxValue": 1e9, "variableFolder": v}
+                                      for v in variables],
+                        "engine": {"isovalues": 40, "bins": 32}}]}
+    (tmp_path / "script.json").write_text(json.dumps(cfg))
+    r = subprocess.run([CLI, "script", str(tmp_path / "script.json")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr + r.stdout
+    meta = json.loads((tmp_path / "out" / "meta.json").read_text())
+    assert len(meta["volumes"]) == 4 and all(len(v["representatives"]) == 16 for v in meta["volumes"])
+    mcfg = {"jsonFile": "meta.json", "timeSteps": steps, "dataRoot": str(tmp_path / "out"), "dfDownscale": 1,
+            "engine": {"bins": 32}}
+    (tmp_path / "multi.json").write_text(json.dumps(mcfg))
+    r = subprocess.run([CLI, "multi", str(tmp_path / "multi.json")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr + r.stdout
+    meta = json.loads((tmp_path / "out" / "meta.json").read_text())
+    names = meta["variables"]
+    cross = [(names[m["var1"]], m["t1"], names[m["var2"]], m["t2"], m["filename"]) for m in meta["similarityMaps"]
+             if m["filename"].endswith(".dat") and "TMP-multiMap" in m["filename"]]
+    assert sorted((a, t1, b, t2) for a, t1, b, t2, _ in cross) == [("A", 0, "A", 1), ("A", 0, "B", 0),
+                                                                   ("A", 1, "B", 1), ("B", 0, "B", 1)]
+    F = 16 ** 3
+    for a, t1, b, t2, f in cross:
+        got = np.fromfile(f, np.float32).reshape(16, 16)
+        fa = [np.fromfile(tmp_path / "out" / ("%s-%d" % (a, t1)) / "distancefields" / ("distancefield-%d.df" % i),
+                          np.float32) for i in range(16)]
+        fb = [np.fromfile(tmp_path / "out" / ("%s-%d" % (b, t2)) / "distancefields" / ("distancefield-%d.df" % i),
+                          np.float32) for i in range(16)]
+        for i in range(16):
+            for j in range(16):
+                joint, _, _ = oracle.pair_histogram(fa[i], fb[j], 32, oracle.field_interval(fa[i]),
+                                                    oracle.field_interval(fb[j]))
+                assert abs(got[i, j] - oracle.mi_f64(joint, F)) < 1e-6
+    r = subprocess.run([CLI, "check", str(tmp_path / "out" / "meta.json"), "0", "2"], capture_output=True, text=True)
+    assert r.returncode == 0 and "0 missing" in r.stdout
