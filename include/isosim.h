@@ -231,6 +231,56 @@ ISO_API int iso_generate_hierarchy_h(const float *points_xyz, long numPoints, in
                                      float *h_distances, int numSamples, int dfDownscale);
 
 /* ---------------------------------------------------------------------- */
+/* Serving loop: device-resident request queue with continuous batching   */
+/* (the reference's batch driver, runtime/src/Scripting.cpp:22-236, runs   */
+/* one volume at a time; this is its concurrent form)                      */
+/* ---------------------------------------------------------------------- */
+
+typedef struct iso_server iso_server;
+
+typedef struct iso_request {
+    const float *volume;      /* X*Y*Z floats, img order, host or device; read while the request runs */
+    int X, Y, Z;
+    const float *isovalues;   /* n floats, host */
+    int n;
+    iso_opts opts;
+    float *ism_out;           /* n*n floats capacity (m*m written), host or device */
+    int32_t *field_ids_out;   /* n entries capacity */
+    int32_t *m_out;           /* may be NULL */
+} iso_request;
+
+typedef struct iso_request_result {
+    int status;
+    int32_t m;
+    double latency_ms;        /* submission to completion */
+    double queue_ms;          /* submission to start */
+    iso_timing timing;        /* GPU stage times */
+} iso_request_result;
+
+typedef struct iso_server_stats {
+    int64_t completed, failed;
+    double p50_ms, p99_ms;    /* request latency percentiles over completed requests */
+    size_t peak_device_bytes; /* highest admitted total */
+    size_t held_device_bytes; /* arenas currently held */
+} iso_server_stats;
+
+/* A pool of `slots` workers on `device`, each with its own stream and arena;
+ * requests run concurrently as workers and device memory free up.  A request
+ * is admitted once its surface count pass fixes its device-memory need and
+ * that need fits the budget next to the running requests (idle arenas are
+ * trimmed to make room; waiting requests go in submission order; a request
+ * larger than the budget fails with ISO_ERR_NOMEM). */
+ISO_API int iso_server_create(int device, int slots, size_t hbm_budget_bytes, iso_server **out);
+/* Queues a request (the descriptor is copied; the buffers must stay valid
+ * until iso_server_wait returns for its ticket). */
+ISO_API int iso_server_submit(iso_server *s, const iso_request *req, int64_t *ticket);
+/* Blocks until the request is done; returns its status. */
+ISO_API int iso_server_wait(iso_server *s, int64_t ticket, iso_request_result *result);
+ISO_API int iso_server_get_stats(iso_server *s, iso_server_stats *out);
+/* Finishes queued requests, then stops the workers. */
+ISO_API void iso_server_destroy(iso_server *s);
+
+/* ---------------------------------------------------------------------- */
 /* Allocation-free similarity map (no counterpart in the reference)        */
 /* ---------------------------------------------------------------------- */
 

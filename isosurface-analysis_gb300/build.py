@@ -27,6 +27,7 @@ SOURCES = [
     "iso_distance.cu",
     "iso_histogram.cu",
     "iso_pipeline.cu",
+    "iso_server.cu",
     "iso_reps.cpp",
 ]
 HEADERS = [os.path.join(CSRC, "iso_internal.cuh"), os.path.join(ROOT, "include", "isosim.h")]

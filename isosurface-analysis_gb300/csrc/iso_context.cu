@@ -54,6 +54,20 @@ extern "C" void iso_ctx_destroy(iso_ctx *ctx)
     delete ctx;
 }
 
+void iso_ctx_release(iso_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (int b = 0; b < BUF_COUNT_; ++b) {
+        if (ctx->buf[b]) cudaFree(ctx->buf[b]);
+        ctx->buf[b] = nullptr;
+        ctx->cap[b] = 0;
+    }
+    ctx->clnc_ready = false;
+    ctx->last_m = 0;
+}
+
 extern "C" void *iso_ctx_stream(iso_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 
 extern "C" int64_t iso_ctx_launches(iso_ctx *ctx) { return ctx ? ctx->launches : 0; }

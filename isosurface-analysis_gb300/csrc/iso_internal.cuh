@@ -92,7 +92,17 @@ struct iso_ctx {
     // shape of the distance-field matrix left by the last iso_ism call
     int last_m = 0;
     int64_t last_F = 0, last_stride = 0;
+    // admission hook: called by iso_ism once the surface counts fix the
+    // request's device-memory need; a non-zero return aborts the request
+    int (*admit)(void *user, size_t bytes) = nullptr;
+    void *admit_user = nullptr;
+    // request shape for the admission estimate (set by iso_ism)
+    int64_t plan_V = 0, plan_stride = 0;
+    int plan_bins = 0, plan_lbvh = 0, plan_volume_copy = 0;
 };
+
+// Frees every arena buffer of a context (the context stays usable).
+void iso_ctx_release(iso_ctx *ctx);
 
 // Ensures buffer `b` holds at least `bytes`; contents are not preserved.
 int iso_buf(iso_ctx *ctx, IsoBuf b, size_t bytes, void **out);

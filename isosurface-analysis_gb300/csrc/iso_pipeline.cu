@@ -153,8 +153,17 @@ extern "C" int iso_ism(iso_ctx *ctx, const float *volume, int X, int Y, int Z, c
         ~EvGuard() { for (int i = 0; i < 4; ++i) cudaEventDestroy(e[i]); }
     } guard{ev};
     ISO_CUDA(cudaEventRecord(ev[0], ctx->stream));
+    const bool dev_vol = iso_is_device_ptr(volume);
     const float *d_vol;
     ISO_TRY(device_volume(ctx, volume, V, &d_vol));
+    {
+        const int ds0 = opts->df_downscale < 1 ? 1 : opts->df_downscale;
+        ctx->plan_V = V;
+        ctx->plan_stride = round_up((int64_t)(X / ds0) * (Y / ds0) * (Z / ds0), 64);
+        ctx->plan_bins = opts->bins;
+        ctx->plan_lbvh = opts->df_method == ISO_DF_LBVH;
+        ctx->plan_volume_copy = dev_vol ? 0 : 1;
+    }
 
     std::vector<int64_t> counts(n), offsets(n);
     std::vector<iso_surface_stats> stats(n);

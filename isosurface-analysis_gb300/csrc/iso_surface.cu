@@ -524,11 +524,26 @@ int iso_run_surfaces(iso_ctx *ctx, const float *d_vol, int X, int Y, int Z, cons
     // regions in sorted order: regular + corner candidates per isovalue
     std::vector<int64_t> reg_off(n), cor_off(n);
     int64_t tot_pts = 0, tot_cor = 0;
+    int nonempty = 0;
     for (int k = 0; k < n; ++k) {
         reg_off[k] = tot_pts;
         cor_off[k] = tot_cor;
         tot_pts += (int64_t)(cnt[4 * k] + cnt[4 * k + 1]);
         tot_cor += (int64_t)cnt[4 * k + 1];
+        nonempty += (cnt[4 * k] + cnt[4 * k + 1]) > 0;
+    }
+    if (ctx->admit) {
+        // device bytes the rest of the request needs, from the exact counts:
+        // points (raw + normalised), corner keys, LBVH arrays (keys, values,
+        // gathered and sorted points, 64-byte nodes, links, flags, sort
+        // temporaries), distance fields, histogram scratch and the map
+        const double P = (double)tot_pts, m = (double)nonempty;
+        double need = 4.0 * ctx->plan_V * ctx->plan_volume_copy + 32.0 * P + 16.0 * tot_cor +
+                      (ctx->plan_lbvh ? 180.0 * P : 0.0) + 4.0 * m * ctx->plan_stride + 12.0 * m * m +
+                      8.0 * 65536 + 16.0 * (1 << 20);
+        need *= 1.15;  // arena growth slack
+        if (ctx->admit(ctx->admit_user, (size_t)need) != 0)
+            return iso_fail(ISO_ERR_NOMEM, "request needs %.0f bytes of device memory; over the budget", need);
     }
     void *d_raw, *d_norm, *d_ck = nullptr, *d_ck2 = nullptr;
     ISO_TRY(iso_buf(ctx, BUF_POINTS_RAW, (size_t)(tot_pts + 1) * sizeof(float4), &d_raw));

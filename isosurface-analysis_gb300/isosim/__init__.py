@@ -54,6 +54,22 @@ class Timing(C.Structure):
                 ("total_ms", C.c_float)]
 
 
+class Request(C.Structure):
+    _fields_ = [("volume", C.c_void_p), ("X", C.c_int), ("Y", C.c_int), ("Z", C.c_int),
+                ("isovalues", C.c_void_p), ("n", C.c_int), ("opts", Opts), ("ism_out", C.c_void_p),
+                ("field_ids_out", C.c_void_p), ("m_out", C.c_void_p)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("m", C.c_int32), ("latency_ms", C.c_double), ("queue_ms", C.c_double),
+                ("timing", Timing)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("completed", C.c_int64), ("failed", C.c_int64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("peak_device_bytes", C.c_size_t), ("held_device_bytes", C.c_size_t)]
+
+
 def _load():
     if not os.path.exists(LIB_PATH):
         raise ImportError("libisosim.so not built (%s); run __graft_entry__.build()" % LIB_PATH)
@@ -81,6 +97,14 @@ def _load():
         "approximate_isosurfaces_h": (C.c_long, [P, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int, P]),
         "iso_marching_cube_h": (C.c_int, [C.c_float, C.c_int, C.c_int, C.c_int, P, C.c_int, P, C.POINTER(C.c_long)]),
         "iso_generate_hierarchy_h": (C.c_int, [P, C.c_long, C.c_int, C.c_int, C.c_int, P, C.c_int, C.c_int]),
+        "iso_transpose_xfastest": (C.c_int, [P, P, C.c_int, C.c_int, C.c_int, P]),
+        "iso_copy_field": (C.c_int, [P, C.c_int, P]),
+        "iso_server_create": (C.c_int, [C.c_int, C.c_int, C.c_size_t, C.POINTER(P)]),
+        "iso_server_submit": (C.c_int, [P, C.POINTER(Request), C.POINTER(C.c_int64)]),
+        "iso_server_wait": (C.c_int, [P, C.c_int64, C.POINTER(RequestResult)]),
+        "iso_server_get_stats": (C.c_int, [P, C.POINTER(ServerStats)]),
+        "iso_server_destroy": (None, [P]),
+        "iso_similarity_map_noalloc": (C.c_int, [P, C.c_int, C.c_int64, C.c_int64, C.c_int, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -236,6 +260,57 @@ class Context:
         size = 0 if vol is None else (vol.numel() if hasattr(vol, "numel") else vol.size)
         _check(lib.iso_isovalues(self.handle, _ptr(vol), size, vmin, vmax, n, 1 if uniform else 0, _ptr(out)))
         return out
+
+
+class Server:
+    """Device-resident request loop: `slots` concurrent workers under an HBM budget."""
+
+    def __init__(self, device=0, slots=4, budget_bytes=150 << 30):
+        h = C.c_void_p()
+        _check(lib.iso_server_create(device, slots, budget_bytes, C.byref(h)))
+        self.handle = h
+        self._live = {}
+
+    def submit(self, volume, dims, isovalues, surface=SURFACE_MC, frame=FRAME_REF, df_method=DF_LBVH,
+               downscale=1, bins=128):
+        X, Y, Z = dims
+        vol = _f32(volume)
+        iso = np.ascontiguousarray(isovalues, dtype=np.float32)
+        n = iso.size
+        ism = np.zeros(n * n, dtype=np.float32)
+        ids = np.zeros(n, dtype=np.int32)
+        m = np.zeros(1, dtype=np.int32)
+        req = Request(_ptr(vol), X, Y, Z, _ptr(iso), n, Opts(surface, frame, df_method, downscale, bins),
+                      _ptr(ism), _ptr(ids), _ptr(m))
+        t = C.c_int64()
+        _check(lib.iso_server_submit(self.handle, C.byref(req), C.byref(t)))
+        self._live[t.value] = (vol, iso, ism, ids, m)
+        return t.value
+
+    def wait(self, ticket):
+        """Returns (ism m x m, ids, RequestResult)."""
+        res = RequestResult()
+        rc = lib.iso_server_wait(self.handle, ticket, C.byref(res))
+        vol, iso, ism, ids, m = self._live.pop(ticket)
+        _check(rc)
+        mm = res.m
+        return ism[: mm * mm].reshape(mm, mm), ids[:mm], res
+
+    def stats(self):
+        st = ServerStats()
+        _check(lib.iso_server_get_stats(self.handle, C.byref(st)))
+        return st
+
+    def close(self):
+        if self.handle:
+            lib.iso_server_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def select_representatives(ism, ids, isovalues, cnt=16):

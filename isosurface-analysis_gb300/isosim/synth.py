@@ -41,7 +41,7 @@ def power_law_field(shape, exponent, seed):
     k[0, 0, 0] = 1.0
     amp = k ** (-exponent / 2.0)
     amp[0, 0, 0] = 0.0
-    field = np.fft.irfftn(spec * amp, s=shape)
+    field = np.fft.irfftn(spec * amp, s=shape, axes=(0, 1, 2))
     field -= field.mean()
     field /= field.std()
     return field.astype(np.float32)

@@ -1,0 +1,73 @@
+"""The serving loop: requests of different shapes, isovalue counts and bins
+run concurrently under an HBM budget, and each result equals the result of
+the same request run alone (bit for bit: every request reads only its own
+buffers)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def requests():
+    import isosim
+    import isosim.synth as synth
+    out = []
+    shapes = [(24, 24, 24), (32, 28, 20), (40, 32, 28), (20, 20, 20), (36, 36, 36), (28, 24, 32)]
+    for k, dims in enumerate(shapes):
+        if k % 2 == 0:
+            vol = synth.gaussian_blobs(dims, 5, 100 + k, sigma=(2.0, 6.0))
+        else:
+            vol = synth.power_law_field(dims, 3.0, 100 + k)
+        n = [8, 16, 12, 24, 10, 20][k]
+        isos = synth.inside_isovalues(vol, n)
+        surface = isosim.SURFACE_APPROX if k == 3 else isosim.SURFACE_MC
+        out.append((vol.ravel(), dims, isos, surface, [32, 64, 128, 16, 256, 64][k]))
+    return out
+
+
+def test_results_same_alone_and_in_the_mix():
+    import isosim
+    reqs = requests()
+    with isosim.Context(0) as ctx:
+        alone = [ctx.ism(v, d, i, surface=s, bins=b)[:2] for v, d, i, s, b in reqs]
+    with isosim.Server(0, slots=3, budget_bytes=2 << 30) as srv:
+        tickets = [srv.submit(v, d, i, surface=s, bins=b) for v, d, i, s, b in reqs * 3]
+        results = [srv.wait(t) for t in tickets]
+        st = srv.stats()
+    for k, (ism, ids, res) in enumerate(results):
+        want_ism, want_ids = alone[k % len(reqs)]
+        assert res.status == 0
+        assert np.array_equal(ids, want_ids)
+        assert np.array_equal(ism, want_ism)
+    assert st.completed == len(tickets) and st.failed == 0
+    assert st.p50_ms > 0 and st.p99_ms >= st.p50_ms
+    assert st.peak_device_bytes <= 2 << 30
+
+
+def test_tight_budget_serialises_but_completes():
+    import isosim
+    reqs = requests()
+    with isosim.Context(0) as ctx:
+        alone = [ctx.ism(v, d, i, surface=s, bins=b)[0] for v, d, i, s, b in reqs]
+    # room for about one request at a time
+    with isosim.Server(0, slots=4, budget_bytes=96 << 20) as srv:
+        tickets = [srv.submit(v, d, i, surface=s, bins=b) for v, d, i, s, b in reqs]
+        for k, t in enumerate(tickets):
+            ism, _, _ = srv.wait(t)
+            assert np.array_equal(ism, alone[k])
+        assert srv.stats().peak_device_bytes <= 96 << 20
+
+
+def test_request_over_budget_fails_cleanly():
+    import isosim
+    import isosim.synth as synth
+    vol = synth.gaussian_blobs((48, 48, 48), 5, 7, sigma=(3.0, 8.0))
+    with isosim.Server(0, slots=2, budget_bytes=24 << 20) as srv:
+        t = srv.submit(vol.ravel(), (48, 48, 48), synth.inside_isovalues(vol, 32), bins=64)
+        with pytest.raises(isosim.IsoError) as e:
+            srv.wait(t)
+        assert e.value.code == isosim.ISO_ERR_NOMEM
+        # the server keeps serving
+        small = synth.gaussian_blobs((16, 16, 16), 3, 8, sigma=(2.0, 4.0))
+        ism, ids, res = srv.wait(srv.submit(small.ravel(), (16, 16, 16), synth.inside_isovalues(small, 4), bins=16))
+        assert res.status == 0 and len(ids) > 0
