@@ -252,11 +252,13 @@ def run_ours(args):
 
 
 def cpu_baseline(vol, isos, bins, sample_scale=1.0):
-    """Reference arithmetic on the host cores over a bounded sample, scaled to
-    one full ISM: marching cubes of a few isovalues, FP32 distance fields of a
-    sample of voxels, joint histograms + NMI of a sample of pairs (the oracle's
-    FP32 histogram/NMI restatement is bit-exact with the reference's
-    calculate_histogram_CPU)."""
+    """The pipeline's CPU arithmetic on all host cores over a bounded sample,
+    scaled to one full ISM (extrapolated):
+      marching cubes of a few isovalues (the oracle's restatement of the
+      reference kernels), distance fields of a random sample of voxels through
+      a k-d tree (exact, same canonical distance), joint histograms + FP32 NMI
+      of a few field pairs (the oracle's restatement, bit-exact with the
+      reference's calculate_histogram_CPU)."""
     from concurrent.futures import ThreadPoolExecutor
 
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -269,42 +271,53 @@ def cpu_baseline(vol, isos, bins, sample_scale=1.0):
     cores = os.cpu_count() or 1
     rng = np.random.default_rng(0)
     k_iso = max(2, int(4 * sample_scale))
-    iso_idx = np.linspace(0, n - 1, k_iso).astype(int)
+    iso_idx = np.linspace(n // 8, n - 1 - n // 8, k_iso).astype(int)
 
-    t0 = time.perf_counter()
+    def mc(i):
+        t0 = time.perf_counter()
+        pts = oracle.marching_cubes(vol, dims, float(isos[i]), frame=0)[0]
+        return pts, time.perf_counter() - t0
+
+    with ThreadPoolExecutor(min(cores, k_iso)) as ex:
+        res = list(ex.map(mc, iso_idx))
+    t_mc = float(np.mean([t for _, t in res]))
+    n_samp = max(1024, int(4096 * sample_scale))
+
+    def df(pts):
+        p = oracle.normalize_points(pts, dims)
+        t0 = time.perf_counter()
+        oracle.distance_field_kd(p, dims, 1, idx=rng.integers(0, F, 1))  # tree build + one query
+        t_build = time.perf_counter() - t0
+        idx = np.random.default_rng(len(pts)).integers(0, F, n_samp)
+        t0 = time.perf_counter()
+        oracle.distance_field_kd(p, dims, 1, idx=idx)
+        t_q = (time.perf_counter() - t0 - t_build) / n_samp
+        return t_build + max(t_q, 0.0) * F
+
+    surfaces = [p for p, _ in res if len(p)]
+    with ThreadPoolExecutor(min(cores, len(surfaces))) as ex:
+        t_df = float(np.mean(list(ex.map(df, surfaces))))
+    k_pairs = max(cores, int(cores * sample_scale))
+    f = np.abs(rng.standard_normal((2, F))).astype(np.float32) * 0.3
+    lo = [oracle.field_interval(x) for x in f]
+
+    def pair(_):
+        t0 = time.perf_counter()
+        joint, cs, rs = oracle.pair_histogram(f[0], f[1], bins, lo[0], lo[1])
+        oracle.mi_f32(joint, cs, rs, F)
+        return time.perf_counter() - t0
+
     with ThreadPoolExecutor(cores) as ex:
-        surfs = list(ex.map(lambda i: oracle.marching_cubes(vol, dims, float(isos[i]), frame=0)[0], iso_idx))
-    t_mc = (time.perf_counter() - t0) / k_iso * min(cores, k_iso)  # per isovalue, one core
-    # distance fields: a random subset of sample points of each surface
-    n_samp = max(256, int(1024 * sample_scale))
-    pts_all = [oracle.normalize_points(p, dims) for p in surfs if len(p)]
-    t0 = time.perf_counter()
-    evals = 0
-    for p in pts_all:
-        # emulate the per-voxel scan: distance of n_samp random grid points to all points
-        sub = rng.integers(0, F, n_samp)
-        s = np.stack([(sub // (Y * Z)) / np.float32(X), ((sub // Z) % Y) / np.float32(Y), (sub % Z) / np.float32(Z)], 1)
-        s = s.astype(np.float32)
-        for q in range(0, n_samp, 64):
-            d = ((s[q:q + 64, None, :] - p[None, :, :]) ** 2).sum(-1).min(1)
-        evals += n_samp * len(p)
-    t_df_eval = (time.perf_counter() - t0) / max(evals, 1)
-    mean_p = np.mean([len(p) for p in pts_all]) if pts_all else 0
-    # histograms: fields from the sampled surfaces' exact DF would be too slow;
-    # use fields of the right size and distribution (the cost is value-independent)
-    k_pairs = max(cores, int(2 * cores * sample_scale))
-    f = np.abs(rng.standard_normal((2, F))).astype(np.float32)
-    t0 = time.perf_counter()
-    with ThreadPoolExecutor(cores) as ex:
-        list(ex.map(lambda _: oracle.pair_histogram(f[0], f[1], bins), range(k_pairs)))
-    wall = time.perf_counter() - t0
-    t_pair = wall / k_pairs  # wall per pair with `cores` threads
+        t_pair = float(np.mean(list(ex.map(pair, range(k_pairs)))))
     pairs = n * (n - 1) // 2
-    t_ism = (n * t_mc / cores) + (F * mean_p * n * t_df_eval / cores) + pairs * t_pair
+    t_ism = (n * (t_mc + t_df) + pairs * t_pair) / cores
     return {"value": round(pairs / t_ism, 4), "unit": "pairs/s", "cores": cores, "kind": "port",
-            "sample": "%d isovalues of marching cubes, %d sample voxels per distance field, %d histogram pairs, "
-                      "scaled to one %d-isovalue ISM (extrapolated)" % (k_iso, n_samp, k_pairs, n),
-            "seconds_per_ism": round(t_ism, 2)}
+            "sample": "%d isovalues of marching cubes, %d k-d-tree distance samples per surface, %d histogram "
+                      "pairs; per-unit single-core times scaled to one %d-isovalue ISM on %d cores (extrapolated)"
+                      % (k_iso, n_samp, k_pairs, n, cores),
+            "seconds_per_ism": round(t_ism, 2),
+            "per_unit_s": {"marching_cubes_per_isovalue": round(t_mc, 4), "distance_field_per_isovalue": round(t_df, 4),
+                           "histogram_nmi_per_pair": round(t_pair, 5)}}
 
 
 def run_reference(args):
@@ -330,6 +343,164 @@ def run_reference(args):
             "cpu_baseline": cb,
             "e2e": {"value": round(v, 4), "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def run_serving(args):
+    """Poisson stream of ISM requests through the serving loop (continuous
+    batching under an HBM budget) and through one-request-at-a-time serving.
+    Shapes, isovalue counts and bins are drawn per request (seeded); volumes
+    come from a small pool of seeded blob and k^-3 fields kept on the device."""
+    import torch
+
+    import isosim
+    import isosim.synth as synth
+
+    rng = np.random.default_rng(5000)
+    shapes = [(64, 64, 64), (128, 128, 128), (192, 128, 128), (256, 256, 256), (600, 248, 248)]
+    pool = {}
+    for k, sh in enumerate(shapes):
+        scale = min(sh) / 64.0
+        pool[(sh, "blobs")] = torch.from_numpy(
+            synth.gaussian_blobs(sh, 8, 5100 + k, sigma=(4.0 * scale, 12.0 * scale)).ravel()).cuda()
+        if np.prod(sh) <= 192 * 128 * 128:
+            pool[(sh, "grf")] = torch.from_numpy(synth.power_law_field(sh, 3.0, 5200 + k).ravel()).cuda()
+    reqs = []
+    t = 0.0
+    for r in range(args.requests):
+        t += rng.exponential(1.0 / args.rate)
+        sh = shapes[rng.integers(len(shapes))]
+        kind = "grf" if (sh, "grf") in pool and rng.random() < 0.5 else "blobs"
+        n = int(rng.choice([16, 32, 64, 128, 256]))
+        bins = int(rng.choice([128, 256]))
+        vol = pool[(sh, kind)]
+        if kind == "grf":
+            isos = np.linspace(-2.5, 2.5, n).astype(np.float32)
+        else:
+            lo, hi = float(vol.min()), float(vol.max())
+            isos = np.array([lo + (i + 1) * (hi - lo) / (n + 1) for i in range(n)], np.float32)
+        reqs.append((t, vol, sh, isos, bins))
+
+    def serve(slots):
+        with isosim.Server(0, slots=slots, budget_bytes=int(args.budget_gb * (1 << 30))) as srv:
+            # warm each worker's arena on a small request
+            for _ in range(slots):
+                srv.wait(srv.submit(pool[(shapes[0], "blobs")], shapes[0], reqs[0][3][:16], bins=128))
+            t0 = time.perf_counter()
+            tickets = []
+            for (at, vol, sh, isos, bins) in reqs:
+                delay = t0 + at - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                tickets.append((srv.submit(vol, sh, isos, bins=bins), time.perf_counter()))
+            pairs, lat, failed = 0, [], 0
+            for tk, _ in tickets:
+                try:
+                    ism, ids, res = srv.wait(tk)
+                except isosim.IsoError:
+                    failed += 1
+                    continue
+                pairs += len(ids) * (len(ids) - 1) // 2
+                lat.append(res.latency_ms)
+            wall = time.perf_counter() - t0
+            st = srv.stats()
+        lat = np.array(lat)
+        return {"pairs_per_s": round(pairs / wall, 1), "wall_s": round(wall, 2), "pairs": int(pairs), "failed": failed,
+                "p50_ms": round(float(np.percentile(lat, 50)), 1), "p99_ms": round(float(np.percentile(lat, 99)), 1),
+                "peak_admitted_gb": round(st.peak_device_bytes / (1 << 30), 2)}
+
+    batched = serve(args.slots)
+    plain = serve(1)
+    line = {"metric": "ISM pairs/sec and p50/p99 latency, serving", "value": batched["pairs_per_s"],
+            "unit": "pairs/s", "n_gpus": 1, "higher_is_better": True, "data": "synthetic (seeded)",
+            "config": {"workload": "Poisson stream of %d requests at %g req/s; shapes %s; isovalues {16..256}; "
+                                   "bins {128,256}; %g GB HBM budget" % (args.requests, args.rate, shapes, args.budget_gb),
+                       "slots": args.slots},
+            "continuous_batching": batched, "one_at_a_time": plain}
+    print(json.dumps(line), flush=True)
+
+
+def run_multi(args):
+    """Multi-volume batch: V variables x T timesteps of 128^3 k^-3 fields
+    advected 0.5 voxel/step and mixed per variable (seeded 4x4 blend + tanh);
+    64 isovalues per volume -> one ISM each, 16 representatives each, then all
+    16x16 cross maps (same variable across timesteps, all variables at equal
+    timesteps) in one batched launch, aggregated into TSM/VSM entries."""
+    import torch
+
+    import isosim
+
+    V, T, S, n, bins, reps = args.variables, args.timesteps, args.size, 64, 128, 16
+    g = torch.Generator(device="cuda").manual_seed(4000)
+    shape = (S, S, S)
+    k = torch.fft.fftfreq(S, device="cuda")
+    kr = torch.fft.rfftfreq(S, device="cuda")
+    kk = torch.sqrt(k[:, None, None] ** 2 + k[None, :, None] ** 2 + kr[None, None, :] ** 2)
+    amp = kk.clamp_min(1e-12) ** -1.5
+    amp[0, 0, 0] = 0
+    bases = [torch.fft.rfftn(torch.randn(shape, generator=g, device="cuda")) * amp for _ in range(4)]
+    vel = torch.randn(3, generator=g, device="cuda")
+    vel = 0.5 * vel / vel.norm()
+    blend = torch.randn(4, 4, generator=g, device="cuda")
+
+    def volume(var, t):
+        phase = torch.exp(-2j * np.pi * t * (vel[0] * k[:, None, None] + vel[1] * k[None, :, None] +
+                                             vel[2] * kr[None, None, :]))
+        fields = [torch.fft.irfftn(b * phase, s=shape) for b in bases]
+        fields = [(f - f.mean()) / f.std() for f in fields]
+        mix = sum(blend[var, j] * fields[j] for j in range(4))
+        return torch.tanh(mix / mix.std()).contiguous().ravel()
+
+    F = S ** 3
+    stride = (F + 63) // 64 * 64
+    rep_fields = torch.zeros((V * T * reps, stride), dtype=torch.float32, device="cuda")
+    ctx = isosim.Context(0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ism_pairs = 0
+    vid = 0
+    for var in range(V):
+        for t in range(T):
+            vol = volume(var, t)
+            lo, hi = float(vol.min()), float(vol.max())
+            isos = np.array([lo + (i + 1) * (hi - lo) / (n + 1) for i in range(n)], np.float32)
+            ism, ids, _, _ = ctx.ism(vol, shape, isos, bins=bins)
+            ism_pairs += len(ids) * (len(ids) - 1) // 2
+            picks = sorted(r[3] for r in isosim.select_representatives(ism, ids, isos, reps))
+            for q, row in enumerate(picks):
+                ctx.copy_field(row, rep_fields[vid * reps + q])
+            vid += 1
+    torch.cuda.synchronize()
+    t_ism = time.perf_counter() - t0
+    blocks = []
+    for var in range(V):
+        for t1 in range(T):
+            for t2 in range(t1 + 1, T):
+                blocks.append((var * T + t1, var * T + t2))
+    for t in range(T):
+        for v1 in range(V):
+            for v2 in range(v1 + 1, V):
+                blocks.append((v1 * T + t, v2 * T + t))
+    pairs = [(a * reps + i, b * reps + j) for a, b in blocks for i in range(reps) for j in range(reps)]
+    R = V * T * reps
+    pmap = torch.zeros((R, R), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ctx.pair_map(rep_fields, pairs, bins=bins, n=F, stride=stride, out=pmap)
+    agg = ctx.block_similarity(pmap, reps, blocks)
+    torch.cuda.synchronize()
+    t_cross = time.perf_counter() - t0
+    total_pairs = ism_pairs + len(pairs)
+    line = {"metric": "ISM + cross-map pairs/sec, multi-volume batch", "value": round(total_pairs / (t_ism + t_cross), 1),
+            "unit": "pairs/s", "n_gpus": 1, "higher_is_better": True, "data": "synthetic (seeded, generated on the GPU)",
+            "config": {"workload": "%d variables x %d timesteps of %d^3, %d isovalues, %d representatives, %d bins"
+                                   % (V, T, S, n, reps, bins), "isms": V * T, "cross_maps": len(blocks)},
+            "ism_stage": {"pairs": int(ism_pairs), "seconds": round(t_ism, 3)},
+            "cross_stage": {"pairs": len(pairs), "seconds": round(t_cross, 3),
+                            "updates_per_s": round(len(pairs) * F / t_cross, 1)},
+            "tsm_vsm_sample": {"first_blocks": [[int(a), int(b), round(float(x), 4), round(float(y), 4)]
+                                                for (a, b), (x, y) in zip(blocks[:4], agg[:4])]}}
+    print(json.dumps(line), flush=True)
+    ctx.close()
 
 
 def run_case(case):
@@ -366,9 +537,21 @@ def main():
     ap.add_argument("--cpu-scale", type=float, default=1.0)
     ap.add_argument("--case", default=None, choices=["hist-small", "pipe-small"],
                     help="run a small fixed case twice and exit (profiling target)")
+    ap.add_argument("--mode", default="single", choices=["single", "serving", "multi"])
+    ap.add_argument("--requests", type=int, default=40)
+    ap.add_argument("--rate", type=float, default=50.0)
+    ap.add_argument("--slots", type=int, default=4)
+    ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--variables", type=int, default=4)
+    ap.add_argument("--timesteps", type=int, default=50)
+    ap.add_argument("--size", type=int, default=128)
     args = ap.parse_args()
     if args.case:
         run_case(args.case)
+    elif args.mode == "serving":
+        run_serving(args)
+    elif args.mode == "multi":
+        run_multi(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

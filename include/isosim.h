@@ -106,6 +106,11 @@ ISO_API const char *iso_last_error(void);
 /* Number of kernel launches issued by this context so far. */
 ISO_API int64_t iso_ctx_launches(iso_ctx *ctx);
 
+/* Tunable limits of a context. */
+#define ISO_LIMIT_LBVH_GROUP_POINTS 1 /* LBVHs are built for groups of surfaces of at most this many
+                                          points (default 2^27), bounding their device memory */
+ISO_API int iso_ctx_set_limit(iso_ctx *ctx, int which, int64_t value);
+
 /* ---------------------------------------------------------------------- */
 /* Whole-volume pipeline (replaces the per-isovalue loop of Single::run,   */
 /* runtime/src/Single.cpp:193-243, and calculate_histogram_W,              */
@@ -129,6 +134,26 @@ ISO_API int iso_ism(iso_ctx *ctx, const float *volume, int X, int Y, int Z,
  * out[i*m + j] = NMI(fields_a[i], fields_b[j]).  fields_*: m*n floats. */
 ISO_API int iso_cross_map(iso_ctx *ctx, const float *fields_a, const float *fields_b, int m, int64_t n,
                           int bins, float *out);
+
+/* Batched cross maps (the multi module over many volume pairs at once):
+ * fields holds R rows of n values (row r at fields + r*stride, host or
+ * device; aligned device rows are used in place).  For every pair
+ * (pairs[2t], pairs[2t+1]) the NMI goes to out[a*R + b] and out[b*R + a]
+ * (out: R*R floats, host or device; other entries are left as they are).
+ * Each pair's histogram uses the union of its two fields' intervals, as
+ * calculate_histogram_h's multi mode does (JointHistogram.cu:127-129). */
+ISO_API int iso_pair_map(iso_ctx *ctx, const float *fields, int R, int64_t n, int64_t stride, int bins,
+                         const int32_t *pairs, int64_t npairs, float *out);
+
+/* Aggregates k x k blocks of a pair map (R x R, host or device) into one
+ * similarity per block: for block (A, B) = (blocks[2q], blocks[2q+1]),
+ * out[2q] = block mean, out[2q+1] = best-match score (mean of row maxima and
+ * of column maxima, averaged).  With one block per (volume, volume) pair of
+ * representative sets this gives the entries of timestep and variable
+ * similarity matrices.  No reference counterpart: the reference stops at the
+ * cross maps (runtime/src/MultiVar.cpp:222-227). */
+ISO_API int iso_block_similarity(iso_ctx *ctx, const float *map, int64_t R, int k, const int32_t *blocks,
+                                 int64_t nblocks, float *out);
 
 /* ---------------------------------------------------------------------- */
 /* Stage entry points                                                      */

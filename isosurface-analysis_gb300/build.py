@@ -28,6 +28,7 @@ SOURCES = [
     "iso_histogram.cu",
     "iso_pipeline.cu",
     "iso_server.cu",
+    "iso_multi.cu",
     "iso_reps.cpp",
 ]
 HEADERS = [os.path.join(CSRC, "iso_internal.cuh"), os.path.join(ROOT, "include", "isosim.h")]

@@ -68,6 +68,19 @@ void iso_ctx_release(iso_ctx *ctx)
     ctx->last_m = 0;
 }
 
+extern "C" int iso_ctx_set_limit(iso_ctx *ctx, int which, int64_t value)
+{
+    if (!ctx) return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: NULL context");
+    switch (which) {
+    case ISO_LIMIT_LBVH_GROUP_POINTS:
+        if (value < 1) return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: group size must be positive");
+        ctx->lbvh_group_points = value;
+        return ISO_OK;
+    default:
+        return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: unknown limit %d", which);
+    }
+}
+
 extern "C" void *iso_ctx_stream(iso_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 
 extern "C" int64_t iso_ctx_launches(iso_ctx *ctx) { return ctx ? ctx->launches : 0; }

@@ -428,6 +428,98 @@ __global__ void __launch_bounds__(QUERY_THREADS) bvh_query_kernel(Bvh b, SampleG
 
 }  // namespace
 
+// One group of surfaces: segments [seg0, seg0 + m) of sg (absolute indices)
+// with counts h_count[0..m), fields written from `fields` (row 0 = seg0).
+static int lbvh_group(iso_ctx *ctx, const SampleGrid &g, Segments sg, const int64_t *h_count, int m, int seg0,
+                      float *fields, int64_t field_stride)
+{
+    std::vector<int64_t> cstart(m);
+    int64_t total = 0;
+    for (int q = 0; q < m; ++q) {
+        cstart[q] = total;
+        total += h_count[q];
+    }
+    if (total >= (int64_t)0x7fffffff) return iso_fail(ISO_ERR_CAPACITY, "too many surface points (%lld)", (long long)total);
+    void *d_cstart, *d_keys, *d_keys2, *d_vals, *d_vals2, *d_compact, *d_leaves, *d_nodes, *d_pn, *d_pl, *d_flags, *d_misc;
+    ISO_TRY(iso_buf(ctx, BUF_STAGING_A, (size_t)m * 2 * sizeof(int64_t), &d_cstart));
+    ISO_TRY(iso_buf(ctx, BUF_SORT_KEYS, (size_t)total * 8, &d_keys));
+    ISO_TRY(iso_buf(ctx, BUF_SORT_KEYS_ALT, (size_t)total * 8, &d_keys2));
+    ISO_TRY(iso_buf(ctx, BUF_SORT_VALS, (size_t)total * 4, &d_vals));
+    ISO_TRY(iso_buf(ctx, BUF_SORT_VALS_ALT, (size_t)total * 4, &d_vals2));
+    ISO_TRY(iso_buf(ctx, BUF_STAGING_B, (size_t)total * sizeof(float4), &d_compact));
+    ISO_TRY(iso_buf(ctx, BUF_BVH_LEAVES, (size_t)total * sizeof(float4), &d_leaves));
+    ISO_TRY(iso_buf(ctx, BUF_BVH_NODES, (size_t)total * sizeof(BvhNode), &d_nodes));
+    ISO_TRY(iso_buf(ctx, BUF_BVH_PARENT, (size_t)total * 2 * sizeof(int), &d_pn));
+    ISO_TRY(iso_buf(ctx, BUF_BVH_FLAGS, (size_t)total * sizeof(unsigned int), &d_flags));
+    ISO_TRY(iso_buf(ctx, BUF_MISC, 256, &d_misc));
+    d_pl = (int *)d_pn + total;
+    std::vector<int64_t> cs2(2 * (size_t)m);
+    for (int q = 0; q < m; ++q) {
+        cs2[q] = cstart[q];
+        cs2[m + q] = h_count[q];
+    }
+    ISO_CUDA(cudaMemcpyAsync(d_cstart, cs2.data(), cs2.size() * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    ISO_CUDA(cudaMemsetAsync(d_flags, 0, (size_t)total * sizeof(unsigned int), ctx->stream));
+    ISO_CUDA(cudaMemsetAsync(d_misc, 0, sizeof(int), ctx->stream));
+    Segments gs = sg;  // segment offsets of this group
+    gs.offset = sg.offset + seg0;
+    gs.count = sg.count + seg0;
+    Bvh b;
+    b.cstart = (const int64_t *)d_cstart;
+    b.ccount = (const int64_t *)d_cstart + m;
+    b.m = m;
+    b.total = total;
+    b.keys = (unsigned long long *)d_keys;
+    b.vals = (unsigned int *)d_vals;
+    b.compact = (float4 *)d_compact;
+    b.leaves = (float4 *)d_leaves;
+    b.nodes = (BvhNode *)d_nodes;
+    b.parent_node = (int *)d_pn;
+    b.parent_leaf = (int *)d_pl;
+    b.flags = (unsigned int *)d_flags;
+    b.error = (int *)d_misc;
+    const unsigned tb = (unsigned)((total + 255) / 256);
+    bvh_keys_kernel<<<tb, 256, 0, ctx->stream>>>(gs, b);
+    ISO_LAUNCHED(ctx);
+    int end_bit = 32;
+    while ((1ll << (end_bit - 32)) < m && end_bit < 64) ++end_bit;
+    cub::DoubleBuffer<unsigned long long> kb((unsigned long long *)d_keys, (unsigned long long *)d_keys2);
+    cub::DoubleBuffer<unsigned int> vb((unsigned int *)d_vals, (unsigned int *)d_vals2);
+    size_t temp_bytes = 0;
+    ISO_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, kb, vb, (int)total, 0, end_bit, ctx->stream));
+    void *d_temp;
+    ISO_TRY(iso_buf(ctx, BUF_CUB_TEMP, temp_bytes, &d_temp));
+    ISO_CUDA(cub::DeviceRadixSort::SortPairs(d_temp, temp_bytes, kb, vb, (int)total, 0, end_bit, ctx->stream));
+    ctx->launches += 4;
+    bvh_gather_kernel<<<tb, 256, 0, ctx->stream>>>(b, vb.Current());
+    ISO_LAUNCHED(ctx);
+    const int64_t total_nodes = total - m;
+    if (total_nodes > 0) {
+        bvh_build_kernel<<<(unsigned)((total_nodes + 255) / 256), 256, 0, ctx->stream>>>(b, kb.Current());
+        ISO_LAUNCHED(ctx);
+        bvh_boxes_kernel<<<tb, 256, 0, ctx->stream>>>(b);
+        ISO_LAUNCHED(ctx);
+    }
+    for (int base = 0; base < m; base += 65535) {
+        const int cnt = m - base < 65535 ? m - base : 65535;
+        Bvh bb = b;
+        bb.cstart = b.cstart + base;
+        bb.ccount = b.ccount + base;
+        // node bases are cstart[s] - s with the group-local s: shift nodes accordingly
+        bb.nodes = b.nodes - base;
+        const int64_t X10 = g.F / (g.Y10 * g.Z10);
+        const int64_t bricks = ((X10 + 7) / 8) * ((g.Y10 + 15) / 16) * ((g.Z10 + 7) / 8);
+        bvh_query_kernel<<<dim3((unsigned)bricks, cnt), QUERY_THREADS, 0, ctx->stream>>>(
+            bb, g, fields + (size_t)base * field_stride, field_stride);
+        ISO_LAUNCHED(ctx);
+    }
+    int err = 0;
+    ISO_CUDA(cudaMemcpyAsync(&err, d_misc, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    ISO_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (err) return iso_fail(ISO_ERR_INTERNAL, "LBVH consistency check failed (code %d)", err);
+    return ISO_OK;
+}
+
 // Distance fields of `num_segments` point sets (normalised points in
 // BUF_POINTS_NORM; segment q has h_seg_count[q] points at h_seg_offset[q]) into
 // BUF_FIELDS rows q (stride field_stride floats), then per-field min/max into
@@ -472,87 +564,17 @@ int iso_run_distance(iso_ctx *ctx, int X, int Y, int Z, int ds, int method, cons
             ISO_LAUNCHED(ctx);
         }
     } else if (method == ISO_DF_LBVH) {
-        std::vector<int64_t> cstart(m);
-        int64_t total = 0;
-        for (int q = 0; q < m; ++q) {
-            cstart[q] = total;
-            total += h_seg_count[q];
+        // surfaces are processed in groups of at most ctx->lbvh_group_points
+        // points (one surface may exceed it alone), which bounds the LBVH
+        // arrays' memory independently of the number of isovalues
+        for (int q0 = 0; q0 < m;) {
+            int q1 = q0;
+            int64_t pts = 0;
+            while (q1 < m && (q1 == q0 || pts + h_seg_count[q1] <= ctx->lbvh_group_points)) pts += h_seg_count[q1++];
+            ISO_TRY(lbvh_group(ctx, g, sg, h_seg_count + q0, q1 - q0, q0, fields + (size_t)q0 * field_stride,
+                               field_stride));
+            q0 = q1;
         }
-        if (total >= (int64_t)0x7fffffff) return iso_fail(ISO_ERR_CAPACITY, "too many surface points (%lld)", (long long)total);
-        void *d_cstart, *d_keys, *d_keys2, *d_vals, *d_vals2, *d_compact, *d_leaves, *d_nodes, *d_pn, *d_pl, *d_flags, *d_misc;
-        ISO_TRY(iso_buf(ctx, BUF_STAGING_A, (size_t)m * 2 * sizeof(int64_t), &d_cstart));
-        ISO_TRY(iso_buf(ctx, BUF_SORT_KEYS, (size_t)total * 8, &d_keys));
-        ISO_TRY(iso_buf(ctx, BUF_SORT_KEYS_ALT, (size_t)total * 8, &d_keys2));
-        ISO_TRY(iso_buf(ctx, BUF_SORT_VALS, (size_t)total * 4, &d_vals));
-        ISO_TRY(iso_buf(ctx, BUF_SORT_VALS_ALT, (size_t)total * 4, &d_vals2));
-        ISO_TRY(iso_buf(ctx, BUF_STAGING_B, (size_t)total * sizeof(float4), &d_compact));
-        ISO_TRY(iso_buf(ctx, BUF_BVH_LEAVES, (size_t)total * sizeof(float4), &d_leaves));
-        ISO_TRY(iso_buf(ctx, BUF_BVH_NODES, (size_t)total * sizeof(BvhNode), &d_nodes));
-        ISO_TRY(iso_buf(ctx, BUF_BVH_PARENT, (size_t)total * 2 * sizeof(int), &d_pn));
-        ISO_TRY(iso_buf(ctx, BUF_BVH_FLAGS, (size_t)total * sizeof(unsigned int), &d_flags));
-        ISO_TRY(iso_buf(ctx, BUF_MISC, 256, &d_misc));
-        d_pl = (int *)d_pn + total;
-        std::vector<int64_t> cs2(2 * (size_t)m);
-        for (int q = 0; q < m; ++q) {
-            cs2[q] = cstart[q];
-            cs2[m + q] = h_seg_count[q];
-        }
-        ISO_CUDA(cudaMemcpyAsync(d_cstart, cs2.data(), cs2.size() * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
-        ISO_CUDA(cudaMemsetAsync(d_flags, 0, (size_t)total * sizeof(unsigned int), ctx->stream));
-        ISO_CUDA(cudaMemsetAsync(d_misc, 0, sizeof(int), ctx->stream));
-        Bvh b;
-        b.cstart = (const int64_t *)d_cstart;
-        b.ccount = (const int64_t *)d_cstart + m;
-        b.m = m;
-        b.total = total;
-        b.keys = (unsigned long long *)d_keys;
-        b.vals = (unsigned int *)d_vals;
-        b.compact = (float4 *)d_compact;
-        b.leaves = (float4 *)d_leaves;
-        b.nodes = (BvhNode *)d_nodes;
-        b.parent_node = (int *)d_pn;
-        b.parent_leaf = (int *)d_pl;
-        b.flags = (unsigned int *)d_flags;
-        b.error = (int *)d_misc;
-        const unsigned tb = (unsigned)((total + 255) / 256);
-        bvh_keys_kernel<<<tb, 256, 0, ctx->stream>>>(sg, b);
-        ISO_LAUNCHED(ctx);
-        int end_bit = 32;
-        while ((1ll << (end_bit - 32)) < m && end_bit < 64) ++end_bit;
-        cub::DoubleBuffer<unsigned long long> kb((unsigned long long *)d_keys, (unsigned long long *)d_keys2);
-        cub::DoubleBuffer<unsigned int> vb((unsigned int *)d_vals, (unsigned int *)d_vals2);
-        size_t temp_bytes = 0;
-        ISO_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, kb, vb, (int)total, 0, end_bit, ctx->stream));
-        void *d_temp;
-        ISO_TRY(iso_buf(ctx, BUF_CUB_TEMP, temp_bytes, &d_temp));
-        ISO_CUDA(cub::DeviceRadixSort::SortPairs(d_temp, temp_bytes, kb, vb, (int)total, 0, end_bit, ctx->stream));
-        ctx->launches += 4;
-        bvh_gather_kernel<<<tb, 256, 0, ctx->stream>>>(b, vb.Current());
-        ISO_LAUNCHED(ctx);
-        const int64_t total_nodes = total - m;
-        if (total_nodes > 0) {
-            bvh_build_kernel<<<(unsigned)((total_nodes + 255) / 256), 256, 0, ctx->stream>>>(b, kb.Current());
-            ISO_LAUNCHED(ctx);
-            bvh_boxes_kernel<<<tb, 256, 0, ctx->stream>>>(b);
-            ISO_LAUNCHED(ctx);
-        }
-        for (int base = 0; base < m; base += 65535) {
-            int cnt = m - base < 65535 ? m - base : 65535;
-            Bvh bb = b;
-            bb.cstart = b.cstart + base;
-            bb.ccount = b.ccount + base;
-            // node bases are cstart[s] - s with the global s: shift nodes accordingly
-            bb.nodes = b.nodes - base;
-            const int64_t X10 = X / ds;
-            const int64_t bricks = ((X10 + 7) / 8) * ((g.Y10 + 15) / 16) * ((g.Z10 + 7) / 8);
-            bvh_query_kernel<<<dim3((unsigned)bricks, cnt), QUERY_THREADS, 0, ctx->stream>>>(
-                bb, g, fields + (size_t)base * field_stride, field_stride);
-            ISO_LAUNCHED(ctx);
-        }
-        int err = 0;
-        ISO_CUDA(cudaMemcpyAsync(&err, d_misc, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-        ISO_CUDA(cudaStreamSynchronize(ctx->stream));
-        if (err) return iso_fail(ISO_ERR_INTERNAL, "LBVH consistency check failed (code %d)", err);
     } else {
         return iso_fail(ISO_ERR_ARG, "unknown distance-field method %d", method);
     }

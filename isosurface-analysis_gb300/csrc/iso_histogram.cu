@@ -442,23 +442,36 @@ int iso_run_similarity(iso_ctx *ctx, const float *d_fields_a, const float *d_fie
                        float *d_ism, uint32_t *d_joint_dump, uint32_t *d_colrow_dump)
 {
     if (m <= 0) return ISO_OK;
-    if (bins < 2 || bins > ISO_MAX_BINS || (bins & 1))
-        return iso_fail(ISO_ERR_ARG, "bins must be even and in [2, %d], got %d", ISO_MAX_BINS, bins);
-    if (stride % 4 != 0 || ((uintptr_t)d_fields_a & 15) || ((uintptr_t)d_fields_b & 15))
-        return iso_fail(ISO_ERR_ARG, "field rows must be 16-byte aligned with a stride multiple of 4");
     const bool symmetric = d_fields_b == nullptr;
-    const float *fb = symmetric ? d_fields_a : d_fields_b;
-    const uint32_t *mmb = symmetric ? d_minmax_a : d_minmax_b;
-
     const size_t max_tasks = symmetric ? (size_t)m * (m + 1) / 2 : (size_t)m * m;
     std::vector<int2> h_tasks(max_tasks);
     int num_tasks = 0;
     build_tasks(m, symmetric, h_tasks.data(), &num_tasks);
+    return iso_run_similarity_tasks(ctx, d_fields_a, symmetric ? d_fields_a : d_fields_b, m, n, stride, bins, d_minmax_a,
+                                    symmetric ? d_minmax_a : d_minmax_b, d_ism, h_tasks.data(), num_tasks,
+                                    symmetric, d_joint_dump, d_colrow_dump);
+}
+
+int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float *d_fields_b, int m, int64_t n,
+                             int64_t stride, int bins, const uint32_t *d_minmax_a, const uint32_t *d_minmax_b,
+                             float *d_ism, const int2 *h_tasks, int64_t num_tasks_in, bool symmetric,
+                             uint32_t *d_joint_dump, uint32_t *d_colrow_dump)
+{
+    if (num_tasks_in <= 0) return ISO_OK;
+    if (num_tasks_in > 0x7fffffff) return iso_fail(ISO_ERR_ARG, "too many pair tasks");
+    if (bins < 2 || bins > ISO_MAX_BINS || (bins & 1))
+        return iso_fail(ISO_ERR_ARG, "bins must be even and in [2, %d], got %d", ISO_MAX_BINS, bins);
+    if (stride % 4 != 0 || ((uintptr_t)d_fields_a & 15) || ((uintptr_t)d_fields_b & 15))
+        return iso_fail(ISO_ERR_ARG, "field rows must be 16-byte aligned with a stride multiple of 4");
+    const float *fb = d_fields_b;
+    const uint32_t *mmb = d_minmax_b;
+    const int num_tasks = (int)num_tasks_in;
+    const size_t max_tasks = (size_t)num_tasks;
 
     void *d_tasks = nullptr, *d_counter = nullptr, *d_events = nullptr, *d_clnc = nullptr;
     ISO_TRY(iso_buf(ctx, BUF_PAIR_TASKS, max_tasks * sizeof(int2), &d_tasks));
     ISO_TRY(iso_buf(ctx, BUF_TASK_COUNTER, 256, &d_counter));
-    ISO_CUDA(cudaMemcpyAsync(d_tasks, h_tasks.data(), num_tasks * sizeof(int2), cudaMemcpyHostToDevice, ctx->stream));
+    ISO_CUDA(cudaMemcpyAsync(d_tasks, h_tasks, (size_t)num_tasks * sizeof(int2), cudaMemcpyHostToDevice, ctx->stream));
     ISO_CUDA(cudaMemsetAsync(d_counter, 0, 2 * sizeof(unsigned int), ctx->stream));
     if (!ctx->clnc_ready) {
         ISO_TRY(iso_buf(ctx, BUF_CLNC, 65536 * sizeof(double), &d_clnc));

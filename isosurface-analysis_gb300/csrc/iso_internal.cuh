@@ -41,6 +41,11 @@ void iso_clear_error();
                             cudaGetErrorString(e__));                                      \
     } while (0)
 
+constexpr int ISO_MAX_BINS = 256;
+// LBVH surfaces are built and queried in groups of at most this many points
+// (default of iso_ctx_set_limit(ISO_LIMIT_LBVH_GROUP_POINTS))
+constexpr int64_t ISO_LBVH_GROUP_POINTS = (int64_t)1 << 27;
+
 // ---------------------------------------------------------------------------
 // device arena: named grow-only buffers owned by a context
 // ---------------------------------------------------------------------------
@@ -94,6 +99,7 @@ struct iso_ctx {
     int64_t last_F = 0, last_stride = 0;
     // admission hook: called by iso_ism once the surface counts fix the
     // request's device-memory need; a non-zero return aborts the request
+    int64_t lbvh_group_points = ISO_LBVH_GROUP_POINTS;  // see iso_ctx_set_limit
     int (*admit)(void *user, size_t bytes) = nullptr;
     void *admit_user = nullptr;
     // request shape for the admission estimate (set by iso_ism)
@@ -148,7 +154,12 @@ int iso_run_similarity(iso_ctx *ctx, const float *d_fields_a, const float *d_fie
                        int64_t n, int64_t stride, int bins, const uint32_t *d_minmax_a,
                        const uint32_t *d_minmax_b, float *d_ism, uint32_t *d_joint_dump,
                        uint32_t *d_colrow_dump);
+// Same, over an explicit list of (i, j) tasks: i indexes fields_a, j fields_b;
+// the result goes to ism[i*m + j] (and [j*m + i] when symmetric).
+int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float *d_fields_b, int m, int64_t n,
+                             int64_t stride, int bins, const uint32_t *d_minmax_a, const uint32_t *d_minmax_b,
+                             float *d_ism, const int2 *h_tasks, int64_t num_tasks, bool symmetric,
+                             uint32_t *d_joint_dump, uint32_t *d_colrow_dump);
 int iso_run_minmax(iso_ctx *ctx, const float *d_fields, int m, int64_t n, int64_t stride, uint32_t *d_minmax);
 
-constexpr int ISO_MAX_BINS = 256;
 constexpr int ISO_MAX_ISOVALUES = 4096;

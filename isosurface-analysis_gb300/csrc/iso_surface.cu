@@ -539,7 +539,8 @@ int iso_run_surfaces(iso_ctx *ctx, const float *d_vol, int X, int Y, int Z, cons
         // temporaries), distance fields, histogram scratch and the map
         const double P = (double)tot_pts, m = (double)nonempty;
         double need = 4.0 * ctx->plan_V * ctx->plan_volume_copy + 32.0 * P + 16.0 * tot_cor +
-                      (ctx->plan_lbvh ? 180.0 * P : 0.0) + 4.0 * m * ctx->plan_stride + 12.0 * m * m +
+                      (ctx->plan_lbvh ? 180.0 * std::min(P, (double)ctx->lbvh_group_points) : 0.0) +
+                      4.0 * m * ctx->plan_stride + 12.0 * m * m +
                       8.0 * 65536 + 16.0 * (1 << 20);
         need *= 1.15;  // arena growth slack
         if (ctx->admit(ctx->admit_user, (size_t)need) != 0)

@@ -81,6 +81,7 @@ def _load():
         "iso_ctx_stream": (P, [P]),
         "iso_ctx_device_bytes": (C.c_size_t, [P]),
         "iso_ctx_launches": (C.c_int64, [P]),
+        "iso_ctx_set_limit": (C.c_int, [P, C.c_int, C.c_int64]),
         "iso_last_error": (C.c_char_p, []),
         "iso_ism": (C.c_int, [P, P, C.c_int, C.c_int, C.c_int, P, C.c_int, C.POINTER(Opts), P, P,
                               C.POINTER(C.c_int32), P, C.POINTER(Timing)]),
@@ -105,6 +106,8 @@ def _load():
         "iso_server_get_stats": (C.c_int, [P, C.POINTER(ServerStats)]),
         "iso_server_destroy": (None, [P]),
         "iso_similarity_map_noalloc": (C.c_int, [P, C.c_int, C.c_int64, C.c_int64, C.c_int, P, P]),
+        "iso_pair_map": (C.c_int, [P, P, C.c_int, C.c_int64, C.c_int64, C.c_int, P, C.c_int64, P]),
+        "iso_block_similarity": (C.c_int, [P, P, C.c_int64, C.c_int, P, C.c_int64, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -172,6 +175,9 @@ class Context:
     def stream(self):
         return lib.iso_ctx_stream(self.handle)
 
+    def set_lbvh_group_points(self, points):
+        _check(lib.iso_ctx_set_limit(self.handle, 1, int(points)))
+
     @property
     def launches(self):
         return int(lib.iso_ctx_launches(self.handle))
@@ -208,6 +214,33 @@ class Context:
         m, n = a.shape
         out = np.zeros((m, m), dtype=np.float32)
         _check(lib.iso_cross_map(self.handle, _ptr(a), _ptr(b), m, n, bins, _ptr(out)))
+        return out
+
+    def pair_map(self, fields, pairs, bins=128, n=None, stride=None, out=None):
+        """NMI of every (a, b) in `pairs` over the rows of `fields` (R x stride).
+        Returns the R x R map (entries outside the pairs stay as `out` had them)."""
+        f = _f32(fields)
+        R = f.shape[0]
+        stride = stride or f.shape[1]
+        n = n or stride
+        p = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
+        if out is None:
+            out = np.zeros((R, R), dtype=np.float32)
+        _check(lib.iso_pair_map(self.handle, _ptr(f), R, n, stride, bins, _ptr(p), p.shape[0], _ptr(out)))
+        return out
+
+    def block_similarity(self, pmap, k, blocks):
+        """(mean, best-match) per k x k block (A, B) of a pair map."""
+        m = _f32(pmap)
+        R = m.shape[0]
+        b = np.ascontiguousarray(blocks, dtype=np.int32).reshape(-1, 2)
+        out = np.zeros((b.shape[0], 2), dtype=np.float32)
+        _check(lib.iso_block_similarity(self.handle, _ptr(m), R, k, _ptr(b), b.shape[0], _ptr(out)))
+        return out
+
+    def copy_field(self, row, out):
+        """Row `row` of the last ism() call's distance-field matrix into `out`."""
+        _check(lib.iso_copy_field(self.handle, row, _ptr(out)))
         return out
 
     # ---- stages -----------------------------------------------------------

@@ -419,6 +419,109 @@ ORC_API void orc_distance_field_f64(const float *pts, long P, int X, int Y, int 
     }
 }
 
+/* k-d tree nearest-point search with the same canonical distance: a subtree
+ * is skipped only when the canonical distance to its box (fma chain over the
+ * per-axis gaps, monotone in every gap) is >= the best so far, so the result
+ * equals the brute-force minimum bit for bit.  Used for larger oracle cases
+ * and for the CPU baseline. */
+typedef struct { float lo[3], hi[3]; int left, right, start, count; } kd_node;
+typedef struct { const float *pts; int *idx; kd_node *nodes; int nn; } kd_tree;
+
+static int kd_build(kd_tree *t, int start, int count)
+{
+    int me = t->nn++;
+    kd_node *n = &t->nodes[me];
+    for (int d = 0; d < 3; ++d) { n->lo[d] = 3.4e38f; n->hi[d] = -3.4e38f; }
+    for (int i = start; i < start + count; ++i)
+        for (int d = 0; d < 3; ++d) {
+            float v = t->pts[3 * t->idx[i] + d];
+            if (v < n->lo[d]) n->lo[d] = v;
+            if (v > n->hi[d]) n->hi[d] = v;
+        }
+    n->start = start; n->count = count; n->left = n->right = -1;
+    if (count <= 8) return me;
+    int axis = 0;
+    for (int d = 1; d < 3; ++d)
+        if (n->hi[d] - n->lo[d] > n->hi[axis] - n->lo[axis]) axis = d;
+    /* quickselect the median on `axis` */
+    int lo = start, hi = start + count - 1, k = start + count / 2;
+    while (lo < hi) {
+        float pivot = t->pts[3 * t->idx[(lo + hi) / 2] + axis];
+        int i = lo, j = hi;
+        while (i <= j) {
+            while (t->pts[3 * t->idx[i] + axis] < pivot) ++i;
+            while (t->pts[3 * t->idx[j] + axis] > pivot) --j;
+            if (i <= j) { int tmp = t->idx[i]; t->idx[i] = t->idx[j]; t->idx[j] = tmp; ++i; --j; }
+        }
+        if (k <= j) hi = j; else if (k >= i) lo = i; else break;
+    }
+    int half = count / 2;
+    int l = kd_build(t, start, half);
+    int r = kd_build(t, start + half, count - half);
+    t->nodes[me].left = l;
+    t->nodes[me].right = r;
+    return me;
+}
+
+static float kd_box_dist(const kd_node *n, const float s[3])
+{
+    float g[3];
+    for (int d = 0; d < 3; ++d) {
+        float a = n->lo[d] - s[d], b = s[d] - n->hi[d];
+        float m = a > b ? a : b;
+        g[d] = m > 0.0f ? m : 0.0f;
+    }
+    return fmaf(g[2], g[2], fmaf(g[1], g[1], g[0] * g[0]));
+}
+
+static float kd_query(const kd_tree *t, const float s[3])
+{
+    float best = 100000.0f;
+    int stack[128], sp = 0;
+    stack[sp++] = 0;
+    while (sp) {
+        const kd_node *n = &t->nodes[stack[--sp]];
+        if (!(kd_box_dist(n, s) < best)) continue;
+        if (n->left < 0) {
+            for (int i = n->start; i < n->start + n->count; ++i) {
+                const float *p = t->pts + 3 * t->idx[i];
+                float dx = s[0] - p[0], dy = s[1] - p[1], dz = s[2] - p[2];
+                float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                if (d2 < best) best = d2;
+            }
+            continue;
+        }
+        float dl = kd_box_dist(&t->nodes[n->left], s), dr = kd_box_dist(&t->nodes[n->right], s);
+        if (dl <= dr) { stack[sp++] = n->right; stack[sp++] = n->left; }
+        else { stack[sp++] = n->left; stack[sp++] = n->right; }
+    }
+    return best;
+}
+
+/* Distance field through the k-d tree; idx (may be NULL for all samples)
+ * selects sample indices, out gets one value per selected sample. */
+ORC_API void orc_distance_field_kd(const float *pts, long P, int X, int Y, int Z, int ds, const long *idx, long cnt,
+                                   float *out)
+{
+    kd_tree t;
+    t.pts = pts;
+    t.idx = (int *)malloc(sizeof(int) * (size_t)P);
+    t.nodes = (kd_node *)malloc(sizeof(kd_node) * (size_t)(2 * P + 1));
+    t.nn = 0;
+    for (long i = 0; i < P; ++i) t.idx[i] = (int)i;
+    kd_build(&t, 0, (int)P);
+    long F = (long)(X / ds) * (Y / ds) * (Z / ds);
+    long total = idx ? cnt : F;
+    for (long q = 0; q < total; ++q) {
+        float s[3];
+        df_sample(idx ? idx[q] : q, X, Y, Z, ds, s);
+        float best = kd_query(&t, s);
+        out[q] = P == 1 ? best : sqrtf(best);
+    }
+    free(t.idx);
+    free(t.nodes);
+}
+
 /* ------------------------------------------------------------------------- */
 /* Isovalues                                                                  */
 /* ------------------------------------------------------------------------- */

@@ -49,6 +49,7 @@ def _load_oracle():
         "orc_normalize_points": (None, [_P, C.c_long, C.c_int, C.c_int, C.c_int, _P]),
         "orc_distance_field_f32": (None, [_P, C.c_long, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
         "orc_distance_field_f64": (None, [_P, C.c_long, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
+        "orc_distance_field_kd": (None, [_P, C.c_long, C.c_int, C.c_int, C.c_int, C.c_int, _P, C.c_long, _P]),
         "orc_real_range": (None, [_P, C.c_long, C.c_float, C.c_float, _P, _P]),
         "orc_isovalues": (None, [_P, C.c_long, C.c_float, C.c_float, C.c_int, C.c_int, _P]),
         "orc_select_representatives": (C.c_int, [_P, C.c_int, _P, _P, C.c_int, _P]),
@@ -146,6 +147,20 @@ def distance_field_f32(pts_norm, dims, ds=1):
     X, Y, Z = dims
     out = np.zeros((X // ds) * (Y // ds) * (Z // ds), np.float32)
     orc.orc_distance_field_f32(_p(p), p.shape[0], X, Y, Z, ds, _p(out))
+    return out
+
+
+def distance_field_kd(pts_norm, dims, ds=1, idx=None):
+    """Canonical FP32 field through a k-d tree (bit-identical to distance_field_f32)."""
+    p = f32(pts_norm).reshape(-1, 3)
+    X, Y, Z = dims
+    if idx is None:
+        out = np.zeros((X // ds) * (Y // ds) * (Z // ds), np.float32)
+        orc.orc_distance_field_kd(_p(p), p.shape[0], X, Y, Z, ds, None, 0, _p(out))
+    else:
+        idx = np.ascontiguousarray(idx, np.int64)
+        out = np.zeros(idx.size, np.float32)
+        orc.orc_distance_field_kd(_p(p), p.shape[0], X, Y, Z, ds, _p(idx), idx.size, _p(out))
     return out
 
 

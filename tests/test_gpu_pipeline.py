@@ -87,3 +87,15 @@ def test_isovalue_selection_and_range(ctx):
     for uniform in (True, False):
         assert np.array_equal(ctx.isovalues(vol.ravel(), lo, hi, 32, uniform),
                               oracle.isovalues(vol, lo, hi, 32, uniform))
+
+
+def test_lbvh_groups_give_the_same_fields():
+    """Distance fields built over many small LBVH groups equal one large group."""
+    import isosim
+    import isosim.synth as synth
+    vol, isos, bins = synth.config1(seed=1003)
+    with isosim.Context(0) as a, isosim.Context(0) as b:
+        b.set_lbvh_group_points(3000)
+        ia, ida, _, _ = a.ism(vol.ravel(), (64, 64, 64), isos, bins=bins)
+        ib, idb, _, _ = b.ism(vol.ravel(), (64, 64, 64), isos, bins=bins)
+    assert np.array_equal(ida, idb) and np.array_equal(ia, ib)
