@@ -68,6 +68,23 @@ void iso_ctx_release(iso_ctx *ctx)
     ctx->last_m = 0;
 }
 
+void iso_ctx_release_except_surfaces(iso_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (int b = 0; b < BUF_COUNT_; ++b) {
+        if (b == BUF_VOLUME || b == BUF_ISO_SORTED || b == BUF_SURF_COUNTS || b == BUF_SURF_CURSOR ||
+            b == BUF_SEG_OFFSET || b == BUF_SEG_COUNT)
+            continue;
+        if (ctx->buf[b]) cudaFree(ctx->buf[b]);
+        ctx->buf[b] = nullptr;
+        ctx->cap[b] = 0;
+    }
+    ctx->clnc_ready = false;
+    ctx->last_m = 0;
+}
+
 extern "C" int iso_ctx_set_limit(iso_ctx *ctx, int which, int64_t value)
 {
     if (!ctx) return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: NULL context");

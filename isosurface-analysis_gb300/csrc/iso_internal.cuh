@@ -109,6 +109,9 @@ struct iso_ctx {
 
 // Frees every arena buffer of a context (the context stays usable).
 void iso_ctx_release(iso_ctx *ctx);
+// Frees every buffer except the ones a request holds between its surface count
+// pass and its admission (staged volume, sorted isovalues, counts, offsets).
+void iso_ctx_release_except_surfaces(iso_ctx *ctx);
 
 // Ensures buffer `b` holds at least `bytes`; contents are not preserved.
 int iso_buf(iso_ctx *ctx, IsoBuf b, size_t bytes, void **out);

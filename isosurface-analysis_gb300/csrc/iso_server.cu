@@ -100,29 +100,50 @@ int admit_cb(void *user, size_t need)
     Worker &me = s->workers[a->self];
     if (need > s->budget) return 1;
     me.state = WState::Waiting;
+    s->cv_mem.notify_all();  // the earliest waiter may have been waiting on this worker
     for (;;) {
         if (s->earliest_waiter(a->self)) {
-            size_t others = s->others_bytes(a->self);
-            if (others + std::max(need, me.held) > s->budget) {
-                // trim idle arenas, then this worker's own, before waiting
-                for (size_t w = 0; w < s->workers.size(); ++w) {
+            auto fits = [&] { return s->others_bytes(a->self) + std::max(need, me.held) <= s->budget; };
+            if (!fits()) {
+                // free memory lazily, cheapest first: idle arenas, then the
+                // arenas of requests waiting behind this one (blocked here, so
+                // their streams are idle; their staged surface buffers stay),
+                // then this request's own leftovers from earlier requests
+                for (size_t w = 0; w < s->workers.size() && !fits(); ++w) {
                     Worker &k = s->workers[w];
                     if (w != a->self && k.state == WState::Idle && k.held > 0) {
                         iso_ctx_release(k.ctx);
                         k.held = 0;
                     }
                 }
-                // this worker's own arena holds the request's staged volume
-                // and counts, so it is admitted against max(need, held)
-                others = s->others_bytes(a->self);
+                for (size_t w = 0; w < s->workers.size() && !fits(); ++w) {
+                    Worker &k = s->workers[w];
+                    if (w != a->self && k.state == WState::Waiting && k.held > 0) {
+                        iso_ctx_release_except_surfaces(k.ctx);
+                        k.held = iso_ctx_device_bytes(k.ctx);
+                    }
+                }
+                if (!fits()) {
+                    iso_ctx_release_except_surfaces(me.ctx);
+                    me.held = iso_ctx_device_bytes(me.ctx);
+                }
             }
-            if (others + std::max(need, me.held) <= s->budget) break;
+            if (fits()) break;
+            // nothing left that will free memory: refuse instead of waiting
+            bool pending = false;
+            for (size_t w = 0; w < s->workers.size(); ++w)
+                if (w != a->self && (s->workers[w].state == WState::Running || s->workers[w].state == WState::Counting))
+                    pending = true;
+            if (!pending) {
+                me.state = WState::Counting;
+                return 1;
+            }
         }
         s->cv_mem.wait(lock);
     }
     me.state = WState::Running;
     me.reserved = need;
-    size_t total = s->others_bytes(a->self) + std::max(need, me.held);
+    const size_t total = s->others_bytes(a->self) + std::max(need, me.held);
     s->peak_bytes = std::max(s->peak_bytes, total);
     return 0;
 }
@@ -173,6 +194,7 @@ void worker_loop(iso_server *s, size_t self)
         s->cv_done.notify_all();
     }
 }
+
 
 }  // namespace
 

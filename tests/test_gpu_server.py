@@ -71,3 +71,23 @@ def test_request_over_budget_fails_cleanly():
         small = synth.gaussian_blobs((16, 16, 16), 3, 8, sigma=(2.0, 4.0))
         ism, ids, res = srv.wait(srv.submit(small.ravel(), (16, 16, 16), synth.inside_isovalues(small, 4), bins=16))
         assert res.status == 0 and len(ids) > 0
+
+
+def test_waiters_do_not_hold_memory_the_earliest_needs():
+    """Workers that finished large requests keep their arenas; when a second
+    wave of large requests waits under a budget that fits one at a time, the
+    waiters must release their arenas so the earliest one can run."""
+    import isosim
+    import isosim.synth as synth
+    dims = (48, 48, 48)
+    vol = synth.gaussian_blobs(dims, 6, 21, sigma=(3.0, 9.0))
+    isos = synth.inside_isovalues(vol, 24)
+    with isosim.Context(0) as ctx:
+        want = ctx.ism(vol.ravel(), dims, isos, bins=64)[0]
+    with isosim.Server(0, slots=3, budget_bytes=100 << 20) as srv:
+        for wave in range(2):
+            tickets = [srv.submit(vol.ravel(), dims, isos, bins=64) for _ in range(3)]
+            for t in tickets:
+                ism, _, _ = srv.wait(t)
+                assert np.array_equal(ism, want)
+        assert srv.stats().peak_device_bytes <= 100 << 20
