@@ -99,3 +99,30 @@ def test_lbvh_groups_give_the_same_fields():
         ia, ida, _, _ = a.ism(vol.ravel(), (64, 64, 64), isos, bins=bins)
         ib, idb, _, _ = b.ism(vol.ravel(), (64, 64, 64), isos, bins=bins)
     assert np.array_equal(ida, idb) and np.array_equal(ia, ib)
+
+
+@pytest.mark.parametrize("surface", [0, 1])
+def test_config1_full_size_matches_oracle(ctx, surface):
+    """The 64^3, 32-isovalue, 128-bin workload at full size: surfaces, distance
+    fields (oracle through its exact k-d tree) and the FP64 similarity map."""
+    from concurrent.futures import ThreadPoolExecutor
+    import isosim.synth as synth
+    vol, isos, bins = synth.config1()
+    dims = (64, 64, 64)
+    ism, ids, stats, _ = ctx.ism(vol.ravel(), dims, isos, surface=surface, bins=bins)
+
+    def field(k):
+        if surface == 0:
+            pts, active, total = oracle.marching_cubes(vol, dims, float(isos[k]), frame=0)
+            assert stats[k].active_voxels == active and stats[k].total_verts == total
+        else:
+            pts = oracle.approximation(vol, dims, float(isos[k])).astype(np.float32)
+        assert stats[k].points == len(pts)
+        return oracle.distance_field_kd(oracle.normalize_points(pts, dims), dims) if len(pts) else None
+
+    with ThreadPoolExecutor(8) as ex:
+        fields = list(ex.map(field, range(len(isos))))
+    want_ids = np.array([k for k, f in enumerate(fields) if f is not None], np.int32)
+    assert np.array_equal(ids, want_ids)
+    want = oracle.similarity_map(np.stack([f for f in fields if f is not None]), bins, mode=0)
+    assert np.abs(ism - want).max() < TOL
