@@ -100,11 +100,14 @@ __global__ void __launch_bounds__(BRUTE_THREADS) df_brute_kernel(Segments sg, Sa
 // LBVH
 // ---------------------------------------------------------------------------
 
-struct BvhNode {    // 64 bytes: both child boxes live in the parent
-    float4 l_lo;    // xyz = left box min,  w = left child (int bits)
-    float4 l_hi;    // xyz = left box max,  w = right child (int bits)
-    float4 r_lo;    // xyz = right box min
-    float4 r_hi;    // xyz = right box max
+// 64-byte node holding both children's boxes pairwise (left, right) so one
+// visit evaluates both box distances with packed float2 arithmetic; the max
+// corner is stored negated (s - hi becomes s + (-hi)).
+struct BvhNode {
+    float4 a;  // lo.x (l, r), lo.y (l, r)
+    float4 b;  // lo.z (l, r), -hi.x (l, r)
+    float4 c;  // -hi.y (l, r), -hi.z (l, r)
+    int4 d;    // left child, right child, unused, unused
 };
 constexpr int LEAF_BIT = (int)0x80000000;
 
@@ -221,8 +224,7 @@ __global__ void bvh_build_kernel(Bvh b, const unsigned long long *sorted_keys)
     const int right = (last == split + 1) ? ((split + 1) | LEAF_BIT) : split + 1;
 
     BvhNode *node = b.nodes + nbase + i;
-    node->l_lo.w = __int_as_float(left);
-    node->l_hi.w = __int_as_float(right);
+    node->d = make_int4(left, right, 0, 0);
     if (left & LEAF_BIT) b.parent_leaf[b.cstart[s] + (left & ~LEAF_BIT)] = i * 2 + 0;
     else b.parent_node[nbase + left] = i * 2 + 0;
     if (right & LEAF_BIT) b.parent_leaf[b.cstart[s] + (right & ~LEAF_BIT)] = i * 2 + 1;
@@ -232,14 +234,13 @@ __global__ void bvh_build_kernel(Bvh b, const unsigned long long *sorted_keys)
 
 __device__ __forceinline__ void store_box(BvhNode *node, int side, float3 lo, float3 hi)
 {
-    // keep the child index stored in .w of l_lo / l_hi
-    if (side == 0) {
-        __stcg(&node->l_lo.x, lo.x); __stcg(&node->l_lo.y, lo.y); __stcg(&node->l_lo.z, lo.z);
-        __stcg(&node->l_hi.x, hi.x); __stcg(&node->l_hi.y, hi.y); __stcg(&node->l_hi.z, hi.z);
-    } else {
-        __stcg(&node->r_lo.x, lo.x); __stcg(&node->r_lo.y, lo.y); __stcg(&node->r_lo.z, lo.z);
-        __stcg(&node->r_hi.x, hi.x); __stcg(&node->r_hi.y, hi.y); __stcg(&node->r_hi.z, hi.z);
-    }
+    float *a = &node->a.x, *b = &node->b.x, *c = &node->c.x;
+    __stcg(a + side, lo.x);
+    __stcg(a + 2 + side, lo.y);
+    __stcg(b + side, lo.z);
+    __stcg(b + 2 + side, -hi.x);
+    __stcg(c + side, -hi.y);
+    __stcg(c + 2 + side, -hi.z);
 }
 
 __global__ void bvh_boxes_kernel(Bvh b)
@@ -261,24 +262,52 @@ __global__ void bvh_boxes_kernel(Bvh b)
         __threadfence();
         if (atomicAdd(&b.flags[nbase + parent], 1u) == 0) return;  // sibling not done yet
         __threadfence();
-        float3 a_lo = make_float3(__ldcg(&node->l_lo.x), __ldcg(&node->l_lo.y), __ldcg(&node->l_lo.z));
-        float3 a_hi = make_float3(__ldcg(&node->l_hi.x), __ldcg(&node->l_hi.y), __ldcg(&node->l_hi.z));
-        float3 c_lo = make_float3(__ldcg(&node->r_lo.x), __ldcg(&node->r_lo.y), __ldcg(&node->r_lo.z));
-        float3 c_hi = make_float3(__ldcg(&node->r_hi.x), __ldcg(&node->r_hi.y), __ldcg(&node->r_hi.z));
-        lo = make_float3(fminf(a_lo.x, c_lo.x), fminf(a_lo.y, c_lo.y), fminf(a_lo.z, c_lo.z));
-        hi = make_float3(fmaxf(a_hi.x, c_hi.x), fmaxf(a_hi.y, c_hi.y), fmaxf(a_hi.z, c_hi.z));
+        const float4 na = __ldcg(&node->a), nb = __ldcg(&node->b), nc = __ldcg(&node->c);
+        lo = make_float3(fminf(na.x, na.y), fminf(na.z, na.w), fminf(nb.x, nb.y));
+        hi = make_float3(-fminf(nb.z, nb.w), -fminf(nc.x, nc.y), -fminf(nc.z, nc.w));
         link = b.parent_node[nbase + parent];
     }
     if (link >= 0) atomicExch(b.error, 1);
 }
 
-// canonical squared distance from s to a box (0 inside)
-__device__ __forceinline__ float box_dist2(float3 s, float3 lo, float3 hi)
+__device__ __forceinline__ float max3f(float a, float b, float c)
 {
-    float gx = fmaxf(fmaxf(__fsub_rn(lo.x, s.x), __fsub_rn(s.x, hi.x)), 0.0f);
-    float gy = fmaxf(fmaxf(__fsub_rn(lo.y, s.y), __fsub_rn(s.y, hi.y)), 0.0f);
-    float gz = fmaxf(fmaxf(__fsub_rn(lo.z, s.z), __fsub_rn(s.z, hi.z)), 0.0f);
-    return iso_dist2(gx, gy, gz);
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Sample point prepared for packed box tests.
+struct Query {
+    float2 sx, sy, sz;     // (s, s) per axis
+    float2 nsx, nsy, nsz;  // (-s, -s)
+};
+
+__device__ __forceinline__ Query make_query(float3 s)
+{
+    Query q;
+    q.sx = make_float2(s.x, s.x);
+    q.sy = make_float2(s.y, s.y);
+    q.sz = make_float2(s.z, s.z);
+    q.nsx = make_float2(-s.x, -s.x);
+    q.nsy = make_float2(-s.y, -s.y);
+    q.nsz = make_float2(-s.z, -s.z);
+    return q;
+}
+
+// Canonical squared distances from the sample to both child boxes (0 inside):
+// per-axis gap max(lo - s, s - hi, 0), then fma(gz,gz, fma(gy,gy, gx*gx)) --
+// the same expression as the point distance, so a leaf (lo = hi = p) gives
+// exactly its canonical distance.
+__device__ __forceinline__ float2 child_dist2(const Query &q, const float4 &a, const float4 &b, const float4 &c)
+{
+    const float2 ux = __fadd2_rn(make_float2(a.x, a.y), q.nsx), vx = __fadd2_rn(q.sx, make_float2(b.z, b.w));
+    const float2 uy = __fadd2_rn(make_float2(a.z, a.w), q.nsy), vy = __fadd2_rn(q.sy, make_float2(c.x, c.y));
+    const float2 uz = __fadd2_rn(make_float2(b.x, b.y), q.nsz), vz = __fadd2_rn(q.sz, make_float2(c.z, c.w));
+    const float2 gx = make_float2(max3f(ux.x, vx.x, 0.0f), max3f(ux.y, vx.y, 0.0f));
+    const float2 gy = make_float2(max3f(uy.x, vy.x, 0.0f), max3f(uy.y, vy.y, 0.0f));
+    const float2 gz = make_float2(max3f(uz.x, vz.x, 0.0f), max3f(uz.y, vz.y, 0.0f));
+    return __ffma2_rn(gz, gz, __ffma2_rn(gy, gy, __fmul2_rn(gx, gx)));
 }
 
 // Query layout: a warp owns an 8 (z) x 4 (y) patch of sample columns and each
@@ -289,34 +318,35 @@ __device__ __forceinline__ float box_dist2(float3 s, float3 lo, float3 hi)
 // the nearest region.
 constexpr int PATCH_Z = 8, PATCH_Y = 4, WARPS_Y = QUERY_THREADS / 32, RUN_X = 8;
 
-__device__ __forceinline__ void load_node(const BvhNode *nodes, int cur, float4 &a0, float4 &a1, float4 &c0, float4 &c1)
+__device__ __forceinline__ void load_node(const BvhNode *nodes, int cur, float4 &a, float4 &b, float4 &c, int4 &d)
 {
-    a0 = __ldg(&nodes[cur].l_lo);
-    a1 = __ldg(&nodes[cur].l_hi);
-    c0 = __ldg(&nodes[cur].r_lo);
-    c1 = __ldg(&nodes[cur].r_hi);
+    a = __ldg(&nodes[cur].a);
+    b = __ldg(&nodes[cur].b);
+    c = __ldg(&nodes[cur].c);
+    d = __ldg(&nodes[cur].d);
 }
 
-// Exact nearest canonical squared distance from sp, starting from bound `best`
-// attained at point bp; returns the minimum and updates bp to its point.
-__device__ __forceinline__ float traverse(const BvhNode *nodes, float3 sp, float best, float3 &bp, int *error)
+// Exact nearest canonical squared distance from the sample, starting from
+// bound `best` attained at point bp; returns the minimum, bp its point.
+__device__ __forceinline__ float traverse(const BvhNode *nodes, const Query &q, float best, float3 &bp, int *error)
 {
     int stack[STACK_DEPTH];
     float sdist[STACK_DEPTH];
     int top = 0;
     int cur = 0;
     for (;;) {
-        float4 a0, a1, c0, c1;
-        load_node(nodes, cur, a0, a1, c0, c1);
-        const int left = __float_as_int(a0.w), right = __float_as_int(a1.w);
-        const float dl = box_dist2(sp, make_float3(a0.x, a0.y, a0.z), make_float3(a1.x, a1.y, a1.z));
-        const float dr = box_dist2(sp, make_float3(c0.x, c0.y, c0.z), make_float3(c1.x, c1.y, c1.z));
+        float4 a, b, c;
+        int4 d;
+        load_node(nodes, cur, a, b, c, d);
+        const float2 dd = child_dist2(q, a, b, c);
+        const int left = d.x, right = d.y;
+        const float dl = dd.x, dr = dd.y;
         // a leaf's box is its point: the box distance is its canonical distance
         bool gl = false, gr = false;
         if (left & LEAF_BIT) {
             if (dl < best) {
                 best = dl;
-                bp = make_float3(a0.x, a0.y, a0.z);
+                bp = make_float3(a.x, a.z, b.x);
             }
         } else {
             gl = dl < best;
@@ -324,7 +354,7 @@ __device__ __forceinline__ float traverse(const BvhNode *nodes, float3 sp, float
         if (right & LEAF_BIT) {
             if (dr < best) {
                 best = dr;
-                bp = make_float3(c0.x, c0.y, c0.z);
+                bp = make_float3(a.y, a.w, b.y);
             }
         } else {
             gr = dr < best;
@@ -385,13 +415,14 @@ __global__ void __launch_bounds__(QUERY_THREADS) bvh_query_kernel(Bvh b, SampleG
     // of five warp neighbours as further candidates (all lanes take part)
     int64_t idx0 = col_valid && x0 < X10 ? (x0 * g.Y10 + y) * g.Z10 + z : 0;
     float3 sp = sample_point(g, idx0);
+    Query qy = make_query(sp);
     int cur = 0, leaf = 0;
     for (int depth = 0; depth < STACK_DEPTH; ++depth) {
-        float4 a0, a1, c0, c1;
-        load_node(nodes, cur, a0, a1, c0, c1);
-        const float dl = box_dist2(sp, make_float3(a0.x, a0.y, a0.z), make_float3(a1.x, a1.y, a1.z));
-        const float dr = box_dist2(sp, make_float3(c0.x, c0.y, c0.z), make_float3(c1.x, c1.y, c1.z));
-        const int next = dl <= dr ? __float_as_int(a0.w) : __float_as_int(a1.w);
+        float4 a, b, c;
+        int4 d;
+        load_node(nodes, cur, a, b, c, d);
+        const float2 dd = child_dist2(qy, a, b, c);
+        const int next = dd.x <= dd.y ? d.x : d.y;
         if (next & LEAF_BIT) {
             leaf = next & ~LEAF_BIT;
             break;
@@ -407,9 +438,9 @@ __global__ void __launch_bounds__(QUERY_THREADS) bvh_query_kernel(Bvh b, SampleG
         const float px = __shfl_xor_sync(0xffffffffu, gp.x, mask);
         const float py = __shfl_xor_sync(0xffffffffu, gp.y, mask);
         const float pz = __shfl_xor_sync(0xffffffffu, gp.z, mask);
-        const float d = iso_dist2(__fsub_rn(sp.x, px), __fsub_rn(sp.y, py), __fsub_rn(sp.z, pz));
-        if (d < best) {
-            best = d;
+        const float dv = iso_dist2(__fsub_rn(sp.x, px), __fsub_rn(sp.y, py), __fsub_rn(sp.z, pz));
+        if (dv < best) {
+            best = dv;
             bp = make_float3(px, py, pz);
         }
     }
@@ -419,9 +450,10 @@ __global__ void __launch_bounds__(QUERY_THREADS) bvh_query_kernel(Bvh b, SampleG
         const int64_t idx = (x * g.Y10 + y) * g.Z10 + z;
         if (k > 0) {
             sp = sample_point(g, idx);
+            qy = make_query(sp);
             best = iso_dist2(__fsub_rn(sp.x, bp.x), __fsub_rn(sp.y, bp.y), __fsub_rn(sp.z, bp.z));
         }
-        best = traverse(nodes, sp, best, bp, b.error);
+        best = traverse(nodes, qy, best, bp, b.error);
         out[idx] = __fsqrt_rn(best);
     }
 }

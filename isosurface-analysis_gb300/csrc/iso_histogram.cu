@@ -66,27 +66,30 @@ __device__ __noinline__ int2 exact_bucket_pair(float mn, float step, int bins, f
     return make_int2(iso_bucket(va, mn, step, bins), iso_bucket(vb, mn, step, bins));
 }
 
-// Both buckets of one voxel through a reciprocal.  q' = RN(RN(v-mn) * RN(1/step))
-// is within 257 * 2^-23 + 2^-15 < 2^-13.5 of RN((v-mn)/step) for q < 257, so
-// floor(q') is the exact bucket unless q' lies within 2^-13 of an integer
-// boundary in [1, bins-1]; then both values take the exact division.  RN(q')
-// comes from adding 1.5 * 2^23 (its integer part lands in the low mantissa
-// bits), which needs q' < 2^22: q' is clamped there first.
+// Both buckets of one voxel through a reciprocal, the two fields as one packed
+// float2.  q' = RN(RN(v-mn) * RN(1/step)) is within 257 * 2^-23 + 2^-15 <
+// 2^-13.5 of RN((v-mn)/step) for q < 257, so floor(q') is the exact bucket
+// unless q' lies within 2^-13 of an integer boundary that matters; then both
+// values take the exact division.  floor(q') comes from adding 1.5 * 2^23 to
+// q' - 0.5 (exact): the integer part lands in the low mantissa bits.  Exact
+// integers q' round to an even neighbour there, but their fraction (0 or 1)
+// sends them to the exact path, except q' = 0, whose floor 0 is right.  Values
+// lie inside the pair interval, so q' < 2^22; anything beyond clamps to the
+// last bucket.
 __device__ __forceinline__ void fast_bucket_pair(const Binner &b, float va, float vb, int &ka, int &kb)
 {
     constexpr float MAGIC = 12582912.0f;  // 1.5 * 2^23
     constexpr int MAGIC_BITS = 0x4B400000;
-    const float qa = fminf(__fmul_rn(__fsub_rn(va, b.mn), b.r), 2097152.0f);
-    const float qb = fminf(__fmul_rn(__fsub_rn(vb, b.mn), b.r), 2097152.0f);
-    const float ma = __fadd_rn(qa, MAGIC), mb = __fadd_rn(qb, MAGIC);
-    const float da = __fsub_rn(qa, __fsub_rn(ma, MAGIC)), db = __fsub_rn(qb, __fsub_rn(mb, MAGIC));
-    const int ra = __float_as_int(ma) - MAGIC_BITS, rb = __float_as_int(mb) - MAGIC_BITS;  // RN(q')
+    const float2 d = __fadd2_rn(make_float2(va, vb), make_float2(-b.mn, -b.mn));
+    const float2 q = __fmul2_rn(d, make_float2(b.r, b.r));
+    const float2 m = __fadd2_rn(__fadd2_rn(q, make_float2(-0.5f, -0.5f)), make_float2(MAGIC, MAGIC));
+    const float2 f = __fadd2_rn(m, make_float2(-MAGIC, -MAGIC));               // floor(q')
+    const float2 fr = __ffma2_rn(f, make_float2(-1.0f, -1.0f), q);             // q' - floor(q'), exact
     const unsigned inner = (unsigned)(b.bins - 1);
-    const bool slow = (fabsf(da) < BUCKET_TOL && (unsigned)(ra - 1) < inner) ||
-                      (fabsf(db) < BUCKET_TOL && (unsigned)(rb - 1) < inner);
-    // floor(q') = RN(q') - (q' < RN(q')); unsigned min keeps any index in range
-    ka = (int)min((unsigned)(ra - (da < 0.0f)), inner);
-    kb = (int)min((unsigned)(rb - (db < 0.0f)), inner);
+    const bool slow = fr.x > 1.0f - BUCKET_TOL || (fr.x < BUCKET_TOL && f.x != 0.0f) ||
+                      fr.y > 1.0f - BUCKET_TOL || (fr.y < BUCKET_TOL && f.y != 0.0f);
+    ka = (int)min((unsigned)(__float_as_int(m.x) - MAGIC_BITS), inner);
+    kb = (int)min((unsigned)(__float_as_int(m.y) - MAGIC_BITS), inner);
     if (slow) {
         const int2 e = exact_bucket_pair(b.mn, b.step, b.bins, va, vb);
         ka = e.x;

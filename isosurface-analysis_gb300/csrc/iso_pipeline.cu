@@ -331,6 +331,24 @@ static int similarity_impl(iso_ctx *ctx, const float *const *field_ptrs, const f
                                    cudaMemcpyDefault, ctx->stream));
     }
     if (mins && maxs) {
+        // caller-supplied intervals (the reference's getInterval values) must
+        // contain the data: the reference would index below its histogram
+        // otherwise (JointHistogram.cu:69-73)
+        ISO_TRY(iso_run_minmax(ctx, f, nf, n, stride, (uint32_t *)d_mm));
+        std::vector<uint32_t> mm((size_t)2 * nf);
+        std::vector<float> hmin(nf), hmax(nf);
+        ISO_CUDA(cudaMemcpyAsync(mm.data(), d_mm, mm.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+        ISO_CUDA(cudaMemcpy(hmin.data(), mins, nf * sizeof(float), cudaMemcpyDefault));
+        ISO_CUDA(cudaMemcpy(hmax.data(), maxs, nf * sizeof(float), cudaMemcpyDefault));
+        ISO_CUDA(cudaStreamSynchronize(ctx->stream));
+        for (int k = 0; k < nf; ++k) {
+            float lo, hi;
+            memcpy(&lo, &mm[2 * k], sizeof lo);
+            memcpy(&hi, &mm[2 * k + 1], sizeof hi);
+            if (!(hmin[k] <= lo) || !(hmax[k] >= hi))
+                return iso_fail(ISO_ERR_ARG, "field %d: interval [%g, %g] does not contain its values [%g, %g]", k,
+                                hmin[k], hmax[k], lo, hi);
+        }
         void *d_tmp;
         ISO_TRY(iso_buf(ctx, BUF_STAGING_B, (size_t)2 * nf * sizeof(float), &d_tmp));
         float *t = (float *)d_tmp;
