@@ -326,12 +326,18 @@ __device__ __forceinline__ void load_node(const BvhNode *nodes, int cur, float4 
     d = __ldg(&nodes[cur].d);
 }
 
-// Exact nearest canonical squared distance from the sample, starting from
-// bound `best` attained at point bp; returns the minimum, bp its point.
-__device__ __forceinline__ float traverse(const BvhNode *nodes, const Query &q, float best, float3 &bp, int *error)
+// Exact nearest canonical squared distance for the 32 samples of a warp,
+// traversed as one packet: every lane evaluates every visited node against its
+// own sample and bound, and a subtree is skipped only when no lane's bound
+// admits it (bounds only decrease, so skipping is safe for every lane).  Node
+// addresses are warp-uniform (one broadcast load per node) and no lane idles.
+// `best` starts as the canonical distance to a real point bp; returns the
+// minimum, bp its point.
+__device__ __forceinline__ float traverse_packet(const BvhNode *nodes, const Query &q, float best, float3 &bp,
+                                                 int *error)
 {
-    int stack[STACK_DEPTH];
-    float sdist[STACK_DEPTH];
+    int stack[STACK_DEPTH];     // warp-uniform node ids
+    float sdist[STACK_DEPTH];   // this lane's distance to each postponed node
     int top = 0;
     int cur = 0;
     for (;;) {
@@ -341,7 +347,6 @@ __device__ __forceinline__ float traverse(const BvhNode *nodes, const Query &q, 
         const float2 dd = child_dist2(q, a, b, c);
         const int left = d.x, right = d.y;
         const float dl = dd.x, dr = dd.y;
-        // a leaf's box is its point: the box distance is its canonical distance
         bool gl = false, gr = false;
         if (left & LEAF_BIT) {
             if (dl < best) {
@@ -359,8 +364,10 @@ __device__ __forceinline__ float traverse(const BvhNode *nodes, const Query &q, 
         } else {
             gr = dr < best;
         }
-        if (gl && gr) {
-            const bool lfirst = dl <= dr;
+        const bool any_l = __any_sync(0xffffffffu, gl), any_r = __any_sync(0xffffffffu, gr);
+        if (any_l && any_r) {
+            // most lanes' nearer child first
+            const bool lfirst = __popc(__ballot_sync(0xffffffffu, dl <= dr)) >= 16;
             if (top == STACK_DEPTH) {
                 atomicExch(error, 2);
                 break;
@@ -369,13 +376,12 @@ __device__ __forceinline__ float traverse(const BvhNode *nodes, const Query &q, 
             sdist[top] = lfirst ? dr : dl;
             ++top;
             cur = lfirst ? left : right;
-        } else if (gl) {
+        } else if (any_l) {
             cur = left;
-        } else if (gr) {
+        } else if (any_r) {
             cur = right;
         } else {
-            // pop the next postponed subtree that can still improve
-            while (top > 0 && !(sdist[top - 1] < best)) --top;
+            while (top > 0 && !__any_sync(0xffffffffu, sdist[top - 1] < best)) --top;
             if (top == 0) break;
             cur = stack[--top];
         }
@@ -413,7 +419,9 @@ __global__ void __launch_bounds__(QUERY_THREADS) bvh_query_kernel(Bvh b, SampleG
 
     // first sample of the run: greedy descent to a leaf, then the greedy points
     // of five warp neighbours as further candidates (all lanes take part)
-    int64_t idx0 = col_valid && x0 < X10 ? (x0 * g.Y10 + y) * g.Z10 + z : 0;
+    // lanes outside the grid follow the nearest in-grid sample (coherent packet)
+    const int64_t yc = y < g.Y10 ? y : g.Y10 - 1, zc = z < g.Z10 ? z : g.Z10 - 1;
+    const int64_t idx0 = ((x0 < X10 ? x0 : X10 - 1) * g.Y10 + yc) * g.Z10 + zc;
     float3 sp = sample_point(g, idx0);
     Query qy = make_query(sp);
     int cur = 0, leaf = 0;
@@ -444,17 +452,20 @@ __global__ void __launch_bounds__(QUERY_THREADS) bvh_query_kernel(Bvh b, SampleG
             bp = make_float3(px, py, pz);
         }
     }
+    // every lane runs every step (the packet traversal needs the whole warp);
+    // lanes past the grid edge repeat a valid sample and do not store
     for (int k = 0; k < RUN_X; ++k) {
         const int64_t x = x0 + k;
-        if (!col_valid || x >= X10) break;
-        const int64_t idx = (x * g.Y10 + y) * g.Z10 + z;
+        if (!__any_sync(0xffffffffu, col_valid && x < X10)) break;
+        const bool valid = col_valid && x < X10;
+        const int64_t idx = ((x < X10 ? x : X10 - 1) * g.Y10 + yc) * g.Z10 + zc;
         if (k > 0) {
             sp = sample_point(g, idx);
             qy = make_query(sp);
             best = iso_dist2(__fsub_rn(sp.x, bp.x), __fsub_rn(sp.y, bp.y), __fsub_rn(sp.z, bp.z));
         }
-        best = traverse(nodes, qy, best, bp, b.error);
-        out[idx] = __fsqrt_rn(best);
+        best = traverse_packet(nodes, qy, best, bp, b.error);
+        if (valid) out[idx] = __fsqrt_rn(best);
     }
 }
 
