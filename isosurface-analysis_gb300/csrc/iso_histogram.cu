@@ -125,9 +125,14 @@ __device__ __noinline__ void log_wrap(int bin, uint32_t sh, uint32_t old, int4 *
 
 __device__ __forceinline__ void count_bin(uint32_t *words, int bin, int4 *ev, int cap, unsigned int *nev, int *error)
 {
-    const uint32_t sh = (uint32_t)(bin & 1) << 4;
-    const uint32_t old = atomicAdd(&words[bin >> 1], 1u << sh);
-    if (__builtin_expect(((old >> sh) & 0xffffu) == 0xffffu, 0)) log_wrap(bin, sh, old, ev, cap, nev, error);
+    // odd bins live in the high half: increment 0x10000 and wrap mask
+    // 0xFFFF0000, even bins 1 and 0xFFFF (integer multiply-adds instead of
+    // shifts keep the ALU pipe free)
+    const uint32_t odd = (uint32_t)bin & 1u;
+    const uint32_t inc = odd * 0xFFFFu + 1u;
+    const uint32_t mask = inc * 0xFFFFu;
+    const uint32_t old = atomicAdd(&words[bin >> 1], inc);
+    if (__builtin_expect((old & mask) == mask, 0)) log_wrap(bin, odd << 4, old, ev, cap, nev, error);
 }
 
 __device__ __forceinline__ double clnc_of(const double *table, unsigned long long c)
