@@ -145,6 +145,8 @@ def run_ours(args):
     X, Y, Z = vol.shape
     method = isosim.DF_LBVH if args.df == "lbvh" else isosim.DF_BRUTE
     ctx = isosim.Context(local)
+    if getattr(args, "hist_seg", None) is not None:
+        ctx.set_hist_segment_values(args.hist_seg)
     stream = torch.cuda.ExternalStream(ctx.stream)
     d_vol = torch.from_numpy(vol.ravel()).to(f"cuda:{local}")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
@@ -208,14 +210,24 @@ def run_ours(args):
     # bytes = each distance field read once + each joint histogram written once
     F = X * Y * Z
     hist_bytes = 4.0 * F * m + 4.0 * bins * bins * pairs
+    seg_values = 0 if args.hist_seg is None else args.hist_seg
     hist_s = stage[2] / 1e3
     peak, peak_kind = load_peaks()
     achieved = hist_bytes / hist_s / 1e9
+    counter_peak = ctx.counter_rate(bins if bins & (bins - 1) == 0 else 256)
+    updates = F * pairs / hist_s
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 5), "traffic": None,
-                "kernel": "joint_histogram_mi_kernel",
+                "frac": round(achieved / peak, 5), "traffic": args.hist_traffic,
+                "kernel": ("joint_histogram_seg_kernel + joint_mi_kernel" if 0 < seg_values < F
+                           else "joint_histogram_mi_kernel"),
                 "peak_source": peak_kind,
-                "updates_per_s": round(F * pairs / hist_s, 1),
+                "note": "unique bytes (each field read once, one bins^2 histogram per pair); the kernel is "
+                        "bound by its counter updates: see smem_atomic",
+                "smem_atomic": {"achieved_updates_per_s": round(updates, 1),
+                                "peak_updates_per_s": round(counter_peak, 1),
+                                "frac": round(updates / counter_peak, 4),
+                                "peak_source": "measured in this run (iso_probe_counter_rate)"},
+                "updates_per_s": round(updates, 1),
                 "stage_ms": {"surfaces": round(stage[0], 3), "distance_fields": round(stage[1], 3),
                              "histograms_nmi": round(stage[2], 3)}}
 
@@ -542,14 +554,21 @@ def run_multi(args):
         pg.destroy_process_group()
 
 
-def run_case(case):
+def run_case(case, hist_seg=None):
     """Small fixed workloads for kernel profiles: 'hist-small' = similarity
     map of 16 distance-like fields of 128^3 values at 256 bins; 'pipe-small' =
-    the 64^3, 32-isovalue, 128-bin pipeline."""
+    the 64^3, 32-isovalue, 128-bin pipeline; 'ism-128' = the 128^3 blob+noise
+    volume with 64 isovalues and 256 bins (distance fields of real surfaces)."""
     import isosim
     import isosim.synth as synth
     ctx = isosim.Context(0)
-    if case == "hist-small":
+    if hist_seg is not None:
+        ctx.set_hist_segment_values(hist_seg)
+    if case == "ism-128":
+        vol, isos, bins = synth.config3(size=128, n=64)
+        for _ in range(2):
+            ctx.ism(vol.ravel(), (128, 128, 128), isos, bins=bins)
+    elif case == "hist-small":
         rng = np.random.default_rng(0)
         n = 128 ** 3
         base = rng.uniform(0, 1, n)
@@ -573,8 +592,12 @@ def main():
     ap.add_argument("--config", type=int, default=3, choices=[1, 2, 3])
     ap.add_argument("--df", default="lbvh", choices=["lbvh", "brute"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--hist-seg", type=int, default=None,
+                    help="segment length of the segment-major histogram schedule (0: fused kernel only)")
+    ap.add_argument("--hist-traffic", type=float, default=None,
+                    help="DRAM bytes per histogram launch from an ncu capture (reported as roofline.traffic)")
     ap.add_argument("--cpu-scale", type=float, default=1.0)
-    ap.add_argument("--case", default=None, choices=["hist-small", "pipe-small"],
+    ap.add_argument("--case", default=None, choices=["hist-small", "pipe-small", "ism-128"],
                     help="run a small fixed case twice and exit (profiling target)")
     ap.add_argument("--mode", default="single", choices=["single", "serving", "multi"])
     ap.add_argument("--requests", type=int, default=40)
@@ -586,7 +609,7 @@ def main():
     ap.add_argument("--size", type=int, default=128)
     args = ap.parse_args()
     if args.case:
-        run_case(args.case)
+        run_case(args.case, args.hist_seg)
     elif args.mode == "serving":
         run_serving(args)
     elif args.mode == "multi":

@@ -109,6 +109,10 @@ ISO_API int64_t iso_ctx_launches(iso_ctx *ctx);
 /* Tunable limits of a context. */
 #define ISO_LIMIT_LBVH_GROUP_POINTS 1 /* LBVHs are built for groups of surfaces of at most this many
                                           points (default 2^27), bounding their device memory */
+#define ISO_LIMIT_HIST_SEGMENT_VALUES 2 /* fields longer than this are histogrammed segment by segment
+                                            (all running pairs on the same slice of their fields);
+                                            0 = never (the default); otherwise a multiple of 4,
+                                            at least 65536 */
 ISO_API int iso_ctx_set_limit(iso_ctx *ctx, int which, int64_t value);
 
 /* ---------------------------------------------------------------------- */
@@ -213,6 +217,12 @@ ISO_API int iso_transpose_xfastest(iso_ctx *ctx, const float *src, int X, int Y,
  * (host or device, (X/ds)(Y/ds)(Z/ds) floats) -- the representative
  * fields the single module writes as distancefield-<k>.df. */
 ISO_API int iso_copy_field(iso_ctx *ctx, int row, float *out);
+
+/* Measures the peak rate of the joint-histogram kernel's counter update on
+ * its own (packed 16-bit shared-memory atomic plus wrap check, random bins,
+ * no bucket arithmetic or loads): the shared-memory-atomic roofline of the
+ * histogram stage.  bins: a power of two in [2, 256]. */
+ISO_API int iso_probe_counter_rate(iso_ctx *ctx, int bins, double *updates_per_s);
 
 /* ---------------------------------------------------------------------- */
 /* Reference-named entry points (drop-in for isosurfaces_cuda/funcs.h)     */

@@ -93,6 +93,11 @@ extern "C" int iso_ctx_set_limit(iso_ctx *ctx, int which, int64_t value)
         if (value < 1) return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: group size must be positive");
         ctx->lbvh_group_points = value;
         return ISO_OK;
+    case ISO_LIMIT_HIST_SEGMENT_VALUES:
+        if (value != 0 && (value < 65536 || value % 4 != 0))
+            return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: segment length must be 0 or a multiple of 4 >= 65536");
+        ctx->hist_segment_values = value;
+        return ISO_OK;
     default:
         return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: unknown limit %d", which);
     }

@@ -6,16 +6,18 @@
 // rows 16-byte aligned).  Per-field interval (min, max) as uint32 float bits
 // (all distance values are >= 0, so bit order is value order).
 //
-// Kernel: persistent CTAs pull unordered pair tasks (i <= j) from a counter.
-// A CTA owns one pair at a time and streams both fields with 128-bit loads.
-// Each voxel's two buckets (exact IEEE division, the reference's binning) form
-// one bin; the bin is counted in shared memory as a 16-bit half of a 32-bit
-// word (bins*bins/2 words: 128 KB at 256 bins).  Every 63488 voxels (fewer than
-// 2^16, so no half can overflow) the packed counts are added into the CTA's
-// private uint32 histogram in global memory (L2-resident).  After the last voxel
-// the CTA reduces that histogram: FP64 sum of c*ln(c) over bins and over the
-// exact integer row and column sums, then NMI = 2I/(hX+hY), written to both
-// (i,j) and (j,i).
+// Kernels: persistent CTAs pull unordered pair tasks (i <= j) from a counter and
+// stream both fields with 128-bit loads.  Each voxel's two buckets (the
+// reference's binning: a fixed-point reciprocal, exact IEEE division where the
+// reciprocal cannot decide) form one bin, counted in shared memory as a 16-bit
+// half of a 32-bit word (bins*bins/2 words: 128 KB at 256 bins).  A half that
+// wraps is seen by the thread whose atomic returned 0xFFFF, which records the
+// exact correction.  Short fields: one CTA per pair, FP64 NMI in the same CTA
+// (joint_histogram_mi_kernel).  Long fields: (segment, pair) tasks add into
+// per-pair global histograms, reduced by joint_mi_kernel.  NMI = 2I/(hX+hY)
+// from FP64 sums of c*ln(c) over the bins and over the exact row and column
+// sums, written to both (i,j) and (j,i).
+#include <algorithm>
 #include <mutex>
 #include <vector>
 
@@ -24,7 +26,6 @@
 namespace {
 
 constexpr int HIST_THREADS = 1024;
-constexpr float BUCKET_TOL = 1.220703125e-4f;  // 2^-13, see fast_bucket
 
 __device__ __forceinline__ float bits_to_float(uint32_t b) { return __uint_as_float(b); }
 
@@ -53,47 +54,86 @@ struct PairArgs {
 struct Binner {
     float mn, step, r;
     int bins;
-    int mode;  // 0: reciprocal with exact fallback, 1: exact division only, 2: step == 0
+    int mode;  // 0: fixed-point reciprocal with exact fallback, 1: exact division only, 2: step == 0
 };
 
 // Exact bucket of JointHistogram.cu:63-75 (IEEE division), clamped to [0, bins).
 __device__ __forceinline__ int exact_bucket(const Binner &b, float v) { return iso_bucket(v, b.mn, b.step, b.bins); }
 
-// Out of line: the exact path is rare and would otherwise cost registers in the
-// streaming loop.
-__device__ __noinline__ int2 exact_bucket_pair(float mn, float step, int bins, float va, float vb)
+// Bins of four voxels by IEEE division.  Out of line: the exact path is rare
+// in mode 0 and would otherwise cost registers in the streaming loop.
+__device__ __noinline__ int4 exact_bins4(float mn, float step, int bins, float4 x, float4 y)
 {
-    return make_int2(iso_bucket(va, mn, step, bins), iso_bucket(vb, mn, step, bins));
+    return make_int4(iso_bucket(x.x, mn, step, bins) * bins + iso_bucket(y.x, mn, step, bins),
+                     iso_bucket(x.y, mn, step, bins) * bins + iso_bucket(y.y, mn, step, bins),
+                     iso_bucket(x.z, mn, step, bins) * bins + iso_bucket(y.z, mn, step, bins),
+                     iso_bucket(x.w, mn, step, bins) * bins + iso_bucket(y.w, mn, step, bins));
 }
 
-// Both buckets of one voxel through a reciprocal, the two fields as one packed
-// float2.  q' = RN(RN(v-mn) * RN(1/step)) is within 257 * 2^-23 + 2^-15 <
-// 2^-13.5 of RN((v-mn)/step) for q < 257, so floor(q') is the exact bucket
-// unless q' lies within 2^-13 of an integer boundary that matters; then both
-// values take the exact division.  floor(q') comes from adding 1.5 * 2^23 to
-// q' - 0.5 (exact): the integer part lands in the low mantissa bits.  Exact
-// integers q' round to an even neighbour there, but their fraction (0 or 1)
-// sends them to the exact path, except q' = 0, whose floor 0 is right.  Values
-// lie inside the pair interval, so q' < 2^22; anything beyond clamps to the
-// last bucket.
-__device__ __forceinline__ void fast_bucket_pair(const Binner &b, float va, float vb, int &ka, int &kb)
+// ---- fixed-point bucket ----------------------------------------------------
+// s = RN(RN(v - mn) * r + 1536), r = RN(1/step), in one packed FMA for two
+// values.  1536 = 1.5 * 2^10, so s lies in [1536, 2048) where the float ulp
+// is 2^-13: the low bits of s are q' = s - 1536 as a fixed-point number with
+// 13 fraction bits, u = bits(s) - bits(1536) = q' * 2^13.
+//
+// q' differs from the reference's quotient q = RN(RN(v - mn) / step) by less
+// than 2^-13: 2^-14 (rounding of s) + q * 2^-24 (r) + 2^-17 (rounding of q,
+// q < 256) <= 1.375 * 2^-14.  So floor(q') = floor(q) unless q' is an integer
+// (u a multiple of 2^13), where q may lie just below it; those values take
+// the division.  u = 0 (v == mn, q = 0) is exact.  Near q = bins both sides
+// clamp to the last bucket, so that boundary needs no check.
+constexpr float FX_BASE = 1536.0f;
+constexpr uint32_t FX_BASE_BITS = 0x44C00000u;
+constexpr int FX_FRAC = 13;
+
+__device__ __forceinline__ float2 fx_pair(float a, float b, float2 neg_mn, float2 r)
 {
-    constexpr float MAGIC = 12582912.0f;  // 1.5 * 2^23
-    constexpr int MAGIC_BITS = 0x4B400000;
-    const float2 d = __fadd2_rn(make_float2(va, vb), make_float2(-b.mn, -b.mn));
-    const float2 q = __fmul2_rn(d, make_float2(b.r, b.r));
-    const float2 m = __fadd2_rn(__fadd2_rn(q, make_float2(-0.5f, -0.5f)), make_float2(MAGIC, MAGIC));
-    const float2 f = __fadd2_rn(m, make_float2(-MAGIC, -MAGIC));               // floor(q')
-    const float2 fr = __ffma2_rn(f, make_float2(-1.0f, -1.0f), q);             // q' - floor(q'), exact
-    const unsigned inner = (unsigned)(b.bins - 1);
-    const bool slow = fr.x > 1.0f - BUCKET_TOL || (fr.x < BUCKET_TOL && f.x != 0.0f) ||
-                      fr.y > 1.0f - BUCKET_TOL || (fr.y < BUCKET_TOL && f.y != 0.0f);
-    ka = (int)min((unsigned)(__float_as_int(m.x) - MAGIC_BITS), inner);
-    kb = (int)min((unsigned)(__float_as_int(m.y) - MAGIC_BITS), inner);
-    if (slow) {
-        const int2 e = exact_bucket_pair(b.mn, b.step, b.bins, va, vb);
-        ka = e.x;
-        kb = e.y;
+    return __ffma2_rn(__fadd2_rn(make_float2(a, b), neg_mn), r, make_float2(FX_BASE, FX_BASE));
+}
+
+__device__ __forceinline__ bool fx_ambiguous(uint32_t u) { return ((u & 0x1FFFu) == 0u) & (u != FX_BASE_BITS); }
+
+// bucket + (FX_BASE_BITS >> 13): the constant is folded into the bin offset
+__device__ __forceinline__ uint32_t fx_bucket_biased(uint32_t u, uint32_t lim) { return min(u >> FX_FRAC, lim); }
+
+// Bins (row = field-1 bucket, column = field-2 bucket) of the four voxels in x, y.
+template <int MODE>
+__device__ __forceinline__ void bins4(const Binner &bn, const float4 &x, const float4 &y, int &b0, int &b1, int &b2,
+                                      int &b3)
+{
+    const int bins = bn.bins;
+    if (MODE == 0) {
+        const float2 nm = make_float2(-bn.mn, -bn.mn), rr = make_float2(bn.r, bn.r);
+        const float2 sx01 = fx_pair(x.x, x.y, nm, rr), sx23 = fx_pair(x.z, x.w, nm, rr);
+        const float2 sy01 = fx_pair(y.x, y.y, nm, rr), sy23 = fx_pair(y.z, y.w, nm, rr);
+        const uint32_t ux0 = __float_as_uint(sx01.x), ux1 = __float_as_uint(sx01.y);
+        const uint32_t ux2 = __float_as_uint(sx23.x), ux3 = __float_as_uint(sx23.y);
+        const uint32_t uy0 = __float_as_uint(sy01.x), uy1 = __float_as_uint(sy01.y);
+        const uint32_t uy2 = __float_as_uint(sy23.x), uy3 = __float_as_uint(sy23.y);
+        const uint32_t kb = FX_BASE_BITS >> FX_FRAC;
+        const uint32_t lim = kb + (uint32_t)(bins - 1);
+        const uint32_t off = kb * (uint32_t)bins + kb;
+        // the outer clamp keeps any input (a value below the interval) inside
+        // the histogram; inside the interval it never acts
+        const uint32_t last = (uint32_t)(bins * bins - 1);
+        b0 = (int)min(fx_bucket_biased(ux0, lim) * (uint32_t)bins + fx_bucket_biased(uy0, lim) - off, last);
+        b1 = (int)min(fx_bucket_biased(ux1, lim) * (uint32_t)bins + fx_bucket_biased(uy1, lim) - off, last);
+        b2 = (int)min(fx_bucket_biased(ux2, lim) * (uint32_t)bins + fx_bucket_biased(uy2, lim) - off, last);
+        b3 = (int)min(fx_bucket_biased(ux3, lim) * (uint32_t)bins + fx_bucket_biased(uy3, lim) - off, last);
+        const bool slow = fx_ambiguous(ux0) | fx_ambiguous(ux1) | fx_ambiguous(ux2) | fx_ambiguous(ux3) |
+                          fx_ambiguous(uy0) | fx_ambiguous(uy1) | fx_ambiguous(uy2) | fx_ambiguous(uy3);
+        if (__builtin_expect(slow, 0)) {
+            const int4 e = exact_bins4(bn.mn, bn.step, bins, x, y);
+            b0 = e.x;
+            b1 = e.y;
+            b2 = e.z;
+            b3 = e.w;
+        }
+    } else {
+        b0 = exact_bucket(bn, x.x) * bins + exact_bucket(bn, y.x);
+        b1 = exact_bucket(bn, x.y) * bins + exact_bucket(bn, y.y);
+        b2 = exact_bucket(bn, x.z) * bins + exact_bucket(bn, y.z);
+        b3 = exact_bucket(bn, x.w) * bins + exact_bucket(bn, y.w);
     }
 }
 
@@ -142,56 +182,80 @@ __device__ __forceinline__ double clnc_of(const double *table, unsigned long lon
     return x * log(x);
 }
 
-template <int MODE>
-__device__ __forceinline__ void bucket_pair(const Binner &b, float va, float vb, int &ka, int &kb)
+// Streams values [v0, v1) of one field pair (v0 a multiple of 4, rows 16-byte
+// aligned) into count(bin).  Two load pairs alternate so that one is in
+// flight while the other is binned.
+template <int MODE, class Count>
+__device__ __forceinline__ void stream_values(const Binner &bn, const float *f1, const float *f2, int64_t v0,
+                                              int64_t v1, const Count &count)
 {
-    if (MODE == 0) {
-        fast_bucket_pair(b, va, vb, ka, kb);
-    } else {
-        ka = b.mode == 2 ? 0 : exact_bucket(b, va);
-        kb = b.mode == 2 ? 0 : exact_bucket(b, vb);
+    const float4 *p1 = reinterpret_cast<const float4 *>(f1 + v0);
+    const float4 *p2 = reinterpret_cast<const float4 *>(f2 + v0);
+    const int n4 = (int)((v1 - v0) >> 2);
+    const int step = (int)blockDim.x;
+    int q = (int)threadIdx.x;
+    float4 xa = make_float4(0.f, 0.f, 0.f, 0.f), ya = xa, xb = xa, yb = xa;
+    if (q < n4) {
+        xa = __ldg(p1 + q);
+        ya = __ldg(p2 + q);
+    }
+    while (q < n4) {
+        const int qb = q + step;
+        if (qb < n4) {
+            xb = __ldg(p1 + qb);
+            yb = __ldg(p2 + qb);
+        }
+        int c0, c1, c2, c3;
+        bins4<MODE>(bn, xa, ya, c0, c1, c2, c3);
+        count(c0);
+        count(c1);
+        count(c2);
+        count(c3);
+        if (qb >= n4) break;
+        const int qa = qb + step;
+        if (qa < n4) {
+            xa = __ldg(p1 + qa);
+            ya = __ldg(p2 + qa);
+        }
+        bins4<MODE>(bn, xb, yb, c0, c1, c2, c3);
+        count(c0);
+        count(c1);
+        count(c2);
+        count(c3);
+        q = qa;
+    }
+    for (int64_t v = v0 + ((int64_t)n4 << 2) + threadIdx.x; v < v1; v += blockDim.x) {
+        const int bin = bn.mode == 2 ? 0 : exact_bucket(bn, f1[v]) * bn.bins + exact_bucket(bn, f2[v]);
+        count(bin);
     }
 }
 
-template <int MODE>
-__device__ __forceinline__ void stream_pair(const Binner &bn, const float *f1, const float *f2, int64_t n,
-                                            uint32_t *words, int4 *ev, int cap, unsigned int *nev, int *error)
+struct EventCount {
+    uint32_t *words;
+    int4 *ev;
+    int cap;
+    unsigned int *nev;
+    int *error;
+    __device__ __forceinline__ void operator()(int bin) const { count_bin(words, bin, ev, cap, nev, error); }
+};
+
+// Interval of one pair: the union of both fields' intervals; step, reciprocal
+// and the bucket mode (JointHistogram.cu:100-120).
+__device__ __forceinline__ Binner make_binner(const uint32_t *mma, const uint32_t *mmb, int i, int j, int bins)
 {
-    const float4 *v1 = reinterpret_cast<const float4 *>(f1);
-    const float4 *v2 = reinterpret_cast<const float4 *>(f2);
-    const int64_t n4 = n >> 2;
-    const int bins = bn.bins;
-    int64_t q = threadIdx.x;
-    float4 x = make_float4(0.f, 0.f, 0.f, 0.f), y = x;
-    if (q < n4) {
-        x = __ldg(v1 + q);
-        y = __ldg(v2 + q);
-    }
-    while (q < n4) {
-        const int64_t qn = q + blockDim.x;
-        float4 xn = x, yn = y;
-        if (qn < n4) {
-            xn = __ldg(v1 + qn);
-            yn = __ldg(v2 + qn);
-        }
-        int a0, b0, a1, b1, a2, b2, a3, b3;
-        bucket_pair<MODE>(bn, x.x, y.x, a0, b0);
-        bucket_pair<MODE>(bn, x.y, y.y, a1, b1);
-        bucket_pair<MODE>(bn, x.z, y.z, a2, b2);
-        bucket_pair<MODE>(bn, x.w, y.w, a3, b3);
-        count_bin(words, a0 * bins + b0, ev, cap, nev, error);
-        count_bin(words, a1 * bins + b1, ev, cap, nev, error);
-        count_bin(words, a2 * bins + b2, ev, cap, nev, error);
-        count_bin(words, a3 * bins + b3, ev, cap, nev, error);
-        x = xn;
-        y = yn;
-        q = qn;
-    }
-    for (int64_t v = (n4 << 2) + threadIdx.x; v < n; v += blockDim.x) {
-        int ka, kb;
-        bucket_pair<MODE>(bn, f1[v], f2[v], ka, kb);
-        count_bin(words, ka * bins + kb, ev, cap, nev, error);
-    }
+    Binner bn;
+    const float mn_i = bits_to_float(mma[2 * i]), mx_i = bits_to_float(mma[2 * i + 1]);
+    const float mn_j = bits_to_float(mmb[2 * j]), mx_j = bits_to_float(mmb[2 * j + 1]);
+    bn.mn = mn_i < mn_j ? mn_i : mn_j;
+    const float mx = mx_i > mx_j ? mx_i : mx_j;
+    bn.step = __fdiv_rn(__fsub_rn(mx, bn.mn), (float)bins);
+    bn.bins = bins;
+    bn.r = __frcp_rn(bn.step);
+    // mode 0 needs a finite interval (every non-NaN value then lies in it) and
+    // a normal, finite step with a finite nonzero reciprocal
+    bn.mode = bn.step == 0.0f ? 2
+              : (isfinite(bn.step) && bn.step >= 1.17549435e-38f && isfinite(bn.r) && bn.r > 0.0f ? 0 : 1);
+    return bn;
 }
 
 __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(PairArgs a)
@@ -226,27 +290,15 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
         const int2 task = a.tasks[t];
         const int i = task.x, j = task.y;
 
-        Binner bn;
-        {
-            const float mn_i = bits_to_float(a.mma[2 * i]), mx_i = bits_to_float(a.mma[2 * i + 1]);
-            const float mn_j = bits_to_float(a.mmb[2 * j]), mx_j = bits_to_float(a.mmb[2 * j + 1]);
-            bn.mn = mn_i < mn_j ? mn_i : mn_j;
-            const float mx = mx_i > mx_j ? mx_i : mx_j;
-            bn.step = __fdiv_rn(__fsub_rn(mx, bn.mn), (float)bins);
-            bn.bins = bins;
-            bn.r = __frcp_rn(bn.step);
-            bn.mode = bn.step == 0.0f ? 2 : (isfinite(bn.r) && bn.step >= 1.17549435e-38f ? 0 : 1);
-        }
+        const Binner bn = make_binner(a.mma, a.mmb, i, j, bins);
 
         const float *f1 = a.fa + (size_t)i * a.stride;
         const float *f2 = a.fb + (size_t)j * a.stride;
-        const float4 *v1 = reinterpret_cast<const float4 *>(f1);
-        const float4 *v2 = reinterpret_cast<const float4 *>(f2);
-        const int64_t n4 = a.n >> 2;
 
         // streaming loop, one load pair in flight ahead of the one being binned
-        if (bn.mode == 0) stream_pair<0>(bn, f1, f2, a.n, words, ev, a.event_cap, &s_nev, a.error);
-        else stream_pair<1>(bn, f1, f2, a.n, words, ev, a.event_cap, &s_nev, a.error);
+        const EventCount cnt{words, ev, a.event_cap, &s_nev, a.error};
+        if (bn.mode == 0) stream_values<0>(bn, f1, f2, 0, a.n, cnt);
+        else stream_values<1>(bn, f1, f2, 0, a.n, cnt);
         __syncthreads();
 
         // ---- wrap corrections: per distinct bin, total correction and its
@@ -377,6 +429,202 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
     }
 }
 
+// ---------------------------------------------------------------------------
+// Segment-major schedule for long fields
+//
+// With fields of many megabytes, pairs running concurrently drift apart along
+// the voxel axis and their working set outgrows L2, so every pair re-reads its
+// fields from DRAM.  Here a task is (voxel segment, pair).  Pairs are taken in
+// groups (32 MB of global histograms); within a group the tasks run segment by
+// segment, so the running CTAs read the same slice of their fields and add
+// into histograms that stay in L2.  A task's shared-memory histogram is added
+// into the pair's global histogram (16-bit wraps corrected directly there);
+// joint_mi_kernel then reduces each global histogram to its NMI.
+// ---------------------------------------------------------------------------
+
+struct SegArgs {
+    const float *fa, *fb;
+    int64_t n, stride;
+    int64_t seg_len;     // values per task and field
+    const uint32_t *mma, *mmb;
+    const int2 *tasks;   // the chunk's pairs
+    int num_pairs, num_segs, bins;
+    int group;           // pairs whose segments run together (their histograms stay in L2)
+    uint32_t *ghist;     // num_pairs x bins*bins
+    unsigned int *counter;
+};
+
+// Wrap corrections straight into the pair's global histogram (see count_bin).
+__device__ __noinline__ void log_wrap_global(uint32_t *gh, int bin, uint32_t odd, uint32_t old)
+{
+    const int lo = bin & ~1, hi = bin | 1;
+    if (!odd) {
+        atomicAdd(&gh[lo], 65536u);
+        atomicAdd(&gh[hi], 0xFFFFFFFFu);  // -1: the carry the high half received
+        if ((old >> 16) == 0xffffu) atomicAdd(&gh[hi], 65536u);
+    } else {
+        atomicAdd(&gh[hi], 65536u);
+    }
+}
+
+__device__ __forceinline__ void count_bin_global(uint32_t *words, int bin, uint32_t *gh)
+{
+    const uint32_t odd = (uint32_t)bin & 1u;
+    const uint32_t inc = odd * 0xFFFFu + 1u;
+    const uint32_t mask = inc * 0xFFFFu;
+    const uint32_t old = atomicAdd(&words[bin >> 1], inc);
+    if (__builtin_expect((old & mask) == mask, 0)) log_wrap_global(gh, bin, odd, old);
+}
+
+struct GlobalCount {
+    uint32_t *words;
+    uint32_t *gh;
+    __device__ __forceinline__ void operator()(int bin) const { count_bin_global(words, bin, gh); }
+};
+
+__global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_seg_kernel(SegArgs a)
+{
+    extern __shared__ uint32_t words[];
+    __shared__ int s_task;
+    const int bins = a.bins;
+    const int nwords = bins * bins / 2;
+    for (int w = threadIdx.x; w < nwords; w += blockDim.x) words[w] = 0;
+    const int total = a.num_pairs * a.num_segs;
+    for (;;) {
+        if (threadIdx.x == 0) s_task = (int)atomicAdd(a.counter, 1u);
+        __syncthreads();
+        const int t = s_task;
+        if (t >= total) break;
+        // task order: groups of `group` pairs; within a group segment by
+        // segment, and within a segment pair by pair
+        int seg, p;
+        {
+            const int per_group = a.group * a.num_segs;
+            const int full = a.num_pairs / a.group;
+            if (t < full * per_group) {
+                const int g = t / per_group, r = t - g * per_group;
+                seg = r / a.group;
+                p = g * a.group + (r - seg * a.group);
+            } else {
+                const int r = t - full * per_group, cnt = a.num_pairs - full * a.group;
+                seg = r / cnt;
+                p = full * a.group + (r - seg * cnt);
+            }
+        }
+        const int2 task = a.tasks[p];
+        const int i = task.x, j = task.y;
+        const Binner bn = make_binner(a.mma, a.mmb, i, j, bins);
+        uint32_t *gh = a.ghist + (size_t)p * bins * bins;
+        const int64_t v0 = (int64_t)seg * a.seg_len;
+        const int64_t v1 = v0 + a.seg_len < a.n ? v0 + a.seg_len : a.n;
+        const float *f1 = a.fa + (size_t)i * a.stride;
+        const float *f2 = a.fb + (size_t)j * a.stride;
+        const GlobalCount cnt{words, gh};
+        if (bn.mode == 0) stream_values<0>(bn, f1, f2, v0, v1, cnt);
+        else stream_values<1>(bn, f1, f2, v0, v1, cnt);
+        __syncthreads();
+        for (int w = threadIdx.x; w < nwords; w += blockDim.x) {
+            const uint32_t val = words[w];
+            if (val) {
+                words[w] = 0;
+                if (val & 0xffffu) atomicAdd(&gh[2 * w], val & 0xffffu);
+                if (val >> 16) atomicAdd(&gh[2 * w + 1], val >> 16);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+struct MiArgs {
+    const int2 *tasks;
+    const uint32_t *ghist;
+    int bins, m, symmetric;
+    int64_t n;
+    const double *clnc;
+    float *ism;
+    uint32_t *joint_dump;
+    uint32_t *colrow_dump;
+};
+
+// One block per pair: marginals and sum(c ln c) of the global histogram, NMI.
+__global__ void __launch_bounds__(256) joint_mi_kernel(MiArgs a)
+{
+    __shared__ unsigned long long s_row[ISO_MAX_BINS], s_col[ISO_MAX_BINS];
+    __shared__ double s_red[3][8];
+    const int p = blockIdx.x;
+    const int2 task = a.tasks[p];
+    const int i = task.x, j = task.y;
+    const int bins = a.bins;
+    const uint32_t *gh = a.ghist + (size_t)p * bins * bins;
+    for (int c = threadIdx.x; c < bins; c += blockDim.x) {
+        s_row[c] = 0;
+        s_col[c] = 0;
+    }
+    __syncthreads();
+    double hxy = 0.0;
+    const bool dump = a.joint_dump != nullptr;
+    for (int idx = threadIdx.x; idx < bins * bins; idx += blockDim.x) {
+        const uint32_t c = gh[idx];
+        const int r = idx / bins, col = idx % bins;
+        if (dump) {
+            a.joint_dump[(((size_t)i * a.m + j) * bins + r) * bins + col] = c;
+            if (a.symmetric && i != j) a.joint_dump[(((size_t)j * a.m + i) * bins + col) * bins + r] = c;
+        }
+        if (!c) continue;
+        hxy -= clnc_of(a.clnc, c);
+        atomicAdd(&s_row[r], (unsigned long long)c);
+        atomicAdd(&s_col[col], (unsigned long long)c);
+    }
+    __syncthreads();
+    double hx = 0.0, hy = 0.0;
+    for (int c = threadIdx.x; c < bins; c += blockDim.x) {
+        const unsigned long long cs = s_col[c], rs = s_row[c];
+        if (cs) hx -= clnc_of(a.clnc, cs);
+        if (rs) hy -= clnc_of(a.clnc, rs);
+        if (a.colrow_dump) {
+            const size_t mm = (size_t)a.m * a.m * bins;
+            const size_t bij = ((size_t)i * a.m + j) * bins, bji = ((size_t)j * a.m + i) * bins;
+            a.colrow_dump[bij + c] = (uint32_t)cs;
+            a.colrow_dump[mm + bij + c] = (uint32_t)rs;
+            if (a.symmetric && i != j) {
+                a.colrow_dump[bji + c] = (uint32_t)rs;
+                a.colrow_dump[mm + bji + c] = (uint32_t)cs;
+            }
+        }
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        hxy += __shfl_xor_sync(0xffffffffu, hxy, o);
+        hx += __shfl_xor_sync(0xffffffffu, hx, o);
+        hy += __shfl_xor_sync(0xffffffffu, hy, o);
+    }
+    if (lane == 0) {
+        s_red[0][warp] = hxy;
+        s_red[1][warp] = hy;
+        s_red[2][warp] = hx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sxy = 0.0, sy = 0.0, sx = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            sxy += s_red[0][w];
+            sy += s_red[1][w];
+            sx += s_red[2][w];
+        }
+        const double N = (double)a.n;
+        const double lnN = log(N);
+        sxy = sxy / N + lnN;
+        sx = sx / N + lnN;
+        sy = sy / N + lnN;
+        const double iXY = sx + sy - sxy;
+        const double val = 2.0 * iXY / (sx + sy);
+        const float out = val != val ? 0.0f : (float)val;
+        a.ism[(size_t)i * a.m + j] = out;
+        if (a.symmetric) a.ism[(size_t)j * a.m + i] = out;
+    }
+}
+
 __global__ void clnc_table_kernel(double *table)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -386,15 +634,28 @@ __global__ void clnc_table_kernel(double *table)
 // Per-field min/max over the first n values: min starts at FLT_MAX and max at
 // FLT_MIN as in types/src/DistanceField.cpp:159-200.  Values are >= 0, so
 // unsigned comparison of the bit patterns orders them.
+// Float order as unsigned keys (negative values below positive ones).
+__device__ __forceinline__ uint32_t minmax_key(float f)
+{
+    const uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+__device__ __forceinline__ uint32_t minmax_key_to_bits(uint32_t k) { return (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k; }
+
+// Field interval of DistanceField.cpp:159-200: min starts at FLT_MAX, max at
+// FLT_MIN, NaN never compares.  Reduced as order keys, then stored as float bits.
 __global__ void field_minmax_kernel(const float *fields, int64_t n, int64_t stride, uint32_t *minmax)
 {
     const int f = blockIdx.y;
     const float *row = fields + (size_t)f * stride;
-    uint32_t lo = 0x7f7fffffu, hi = 0x00800000u;
+    uint32_t lo = 0xff7fffffu, hi = 0x80800000u;  // keys of FLT_MAX and FLT_MIN
     for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-        uint32_t b = __float_as_uint(row[v]);
-        lo = b < lo ? b : lo;
-        hi = b > hi ? b : hi;
+        const float x = row[v];
+        if (x != x) continue;
+        const uint32_t k = minmax_key(x);
+        lo = k < lo ? k : lo;
+        hi = k > hi ? k : hi;
     }
     for (int o = 16; o > 0; o >>= 1) {
         uint32_t l2 = __shfl_xor_sync(0xffffffffu, lo, o), h2 = __shfl_xor_sync(0xffffffffu, hi, o);
@@ -411,8 +672,17 @@ __global__ void minmax_init_kernel(uint32_t *minmax, int m)
 {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f < m) {
-        minmax[2 * f] = 0x7f7fffffu;
-        minmax[2 * f + 1] = 0x00800000u;
+        minmax[2 * f] = 0xff7fffffu;
+        minmax[2 * f + 1] = 0x80800000u;
+    }
+}
+
+__global__ void minmax_finish_kernel(uint32_t *minmax, int m)
+{
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f < m) {
+        minmax[2 * f] = minmax_key_to_bits(minmax[2 * f]);
+        minmax[2 * f + 1] = minmax_key_to_bits(minmax[2 * f + 1]);
     }
 }
 
@@ -427,6 +697,8 @@ int iso_run_minmax(iso_ctx *ctx, const float *d_fields, int m, int64_t n, int64_
     int bx = (int)(per < 64 ? per : 64);
     if (bx < 1) bx = 1;
     field_minmax_kernel<<<dim3(bx, m), 256, 0, ctx->stream>>>(d_fields, n, stride, d_minmax);
+    ISO_LAUNCHED(ctx);
+    minmax_finish_kernel<<<(m + 255) / 256, 256, 0, ctx->stream>>>(d_minmax, m);
     ISO_LAUNCHED(ctx);
     return ISO_OK;
 }
@@ -490,6 +762,64 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
     d_clnc = ctx->buf[BUF_CLNC];
 
     const size_t smem = (size_t)bins * bins / 2 * sizeof(uint32_t);
+    const int64_t seg_len = ctx->hist_segment_values;
+    if (seg_len > 0 && n > seg_len) {
+        // long fields: segment-major schedule, pairs in chunks bounding the
+        // global histograms to about 2 GB (and the task count to int range)
+        ISO_CUDA(cudaFuncSetAttribute(joint_histogram_seg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(ISO_MAX_BINS * ISO_MAX_BINS / 2 * sizeof(uint32_t))));
+        const size_t hist_bytes = (size_t)bins * bins * sizeof(uint32_t);
+        const int64_t num_segs64 = (n + seg_len - 1) / seg_len;
+        if (num_segs64 > (1 << 24)) return iso_fail(ISO_ERR_ARG, "histogram segments: %lld too many", (long long)num_segs64);
+        const int num_segs = (int)num_segs64;
+        size_t chunk_sz = std::min<size_t>((size_t)num_tasks, ((size_t)2 << 30) / hist_bytes);
+        chunk_sz = std::min<size_t>(chunk_sz, (size_t)(((int64_t)1 << 30) / num_segs64));
+        const int chunk = (int)std::max<size_t>(1, chunk_sz);
+        const int group = (int)std::max<size_t>(1, std::min<size_t>(1024, ((size_t)32 << 20) / hist_bytes));
+        void *d_gh;
+        ISO_TRY(iso_buf(ctx, BUF_HIST_DUMP_SEG, (size_t)chunk * hist_bytes, &d_gh));
+        int per_sm_seg = 0;
+        ISO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_seg, joint_histogram_seg_kernel, HIST_THREADS, smem));
+        if (per_sm_seg < 1) per_sm_seg = 1;
+        for (int c0 = 0; c0 < num_tasks; c0 += chunk) {
+            const int np = std::min(chunk, num_tasks - c0);
+            ISO_CUDA(cudaMemsetAsync(d_gh, 0, (size_t)np * hist_bytes, ctx->stream));
+            ISO_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned int), ctx->stream));
+            SegArgs sa;
+            sa.fa = d_fields_a;
+            sa.fb = fb;
+            sa.n = n;
+            sa.stride = stride;
+            sa.seg_len = seg_len;
+            sa.mma = d_minmax_a;
+            sa.mmb = mmb;
+            sa.tasks = (const int2 *)d_tasks + c0;
+            sa.num_pairs = np;
+            sa.num_segs = num_segs;
+            sa.bins = bins;
+            sa.group = std::min(group, np);
+            sa.ghist = (uint32_t *)d_gh;
+            sa.counter = (unsigned int *)d_counter;
+            const int64_t seg_tasks = (int64_t)np * num_segs;
+            const int grid_seg = (int)std::min<int64_t>((int64_t)ctx->num_sms * per_sm_seg, seg_tasks);
+            joint_histogram_seg_kernel<<<grid_seg, HIST_THREADS, smem, ctx->stream>>>(sa);
+            ISO_LAUNCHED(ctx);
+            MiArgs ma;
+            ma.tasks = (const int2 *)d_tasks + c0;
+            ma.ghist = (const uint32_t *)d_gh;
+            ma.bins = bins;
+            ma.m = m;
+            ma.symmetric = symmetric ? 1 : 0;
+            ma.n = n;
+            ma.clnc = (const double *)d_clnc;
+            ma.ism = d_ism;
+            ma.joint_dump = d_joint_dump;
+            ma.colrow_dump = d_colrow_dump;
+            joint_mi_kernel<<<np, 256, 0, ctx->stream>>>(ma);
+            ISO_LAUNCHED(ctx);
+        }
+        return ISO_OK;
+    }
     ISO_CUDA(cudaFuncSetAttribute(joint_histogram_mi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)(ISO_MAX_BINS * ISO_MAX_BINS / 2 * sizeof(uint32_t))));
     int per_sm = 0;
@@ -658,6 +988,8 @@ extern "C" int iso_similarity_map_noalloc(const float *d_fields, int m, int64_t 
         const int bx = (int)(per < 64 ? (per < 1 ? 1 : per) : 64);
         field_minmax_kernel<<<dim3(bx, m), 256, 0, st>>>(d_fields, n, stride, minmax);
         ISO_CUDA(cudaGetLastError());
+        minmax_finish_kernel<<<(m + 255) / 256, 256, 0, st>>>(minmax, m);
+        ISO_CUDA(cudaGetLastError());
     }
     PairArgs a;
     a.fa = d_fields;
@@ -687,5 +1019,78 @@ extern "C" int iso_similarity_map_noalloc(const float *d_fields, int m, int64_t 
     ISO_CUDA(cudaMemcpyAsync(&err, ctrl + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
     ISO_CUDA(cudaStreamSynchronize(st));
     if (err) return iso_fail(ISO_ERR_INTERNAL, "iso_similarity_map_noalloc: wrap-event list overflow (code %d)", err);
+    return ISO_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Calibration: the peak rate of the histogram's counter update alone
+// ---------------------------------------------------------------------------
+
+namespace {
+
+// Every thread draws pseudo-random bins from a 32-bit LCG and counts them
+// with the same packed 16-bit atomic and wrap check as the histogram kernel,
+// without bucket arithmetic or global loads.  Wrap corrections are skipped
+// (the counts are discarded); the shared words are summed into `sink` so the
+// work is not removed.
+__global__ void __launch_bounds__(HIST_THREADS, 1) atomic_rate_kernel(int iters, int bins, unsigned int *sink)
+{
+    extern __shared__ uint32_t words[];
+    const int nwords = bins * bins / 2;
+    for (int w = threadIdx.x; w < nwords; w += blockDim.x) words[w] = 0;
+    __syncthreads();
+    uint32_t x = (blockIdx.x * blockDim.x + threadIdx.x) * 2654435761u + 12345u;
+    const uint32_t mask_bins = (uint32_t)(bins * bins - 1);
+    uint32_t wraps = 0;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            x = x * 1664525u + 1013904223u;
+            const uint32_t bin = (x >> 8) & mask_bins;
+            const uint32_t odd = bin & 1u;
+            const uint32_t inc = odd * 0xFFFFu + 1u;
+            const uint32_t mask = inc * 0xFFFFu;
+            const uint32_t old = atomicAdd(&words[bin >> 1], inc);
+            wraps += (old & mask) == mask;
+        }
+    }
+    __syncthreads();
+    uint32_t acc = wraps;
+    for (int w = threadIdx.x; w < nwords; w += blockDim.x) acc += words[w];
+    atomicAdd(sink, acc);
+}
+
+}  // namespace
+
+extern "C" int iso_probe_counter_rate(iso_ctx *ctx, int bins, double *updates_per_s)
+{
+    iso_clear_error();
+    if (!ctx || !updates_per_s || bins < 2 || bins > ISO_MAX_BINS || (bins & (bins - 1)))
+        return iso_fail(ISO_ERR_ARG, "iso_probe_counter_rate: bins must be a power of two in [2, %d]", ISO_MAX_BINS);
+    ISO_CUDA(cudaSetDevice(ctx->device));
+    void *d_sink;
+    ISO_TRY(iso_buf(ctx, BUF_MISC, 256, &d_sink));
+    const size_t smem = (size_t)bins * bins / 2 * sizeof(uint32_t);
+    ISO_CUDA(cudaFuncSetAttribute(atomic_rate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(ISO_MAX_BINS * ISO_MAX_BINS / 2 * sizeof(uint32_t))));
+    const int grid = ctx->num_sms;
+    const int iters = 4096;
+    cudaEvent_t e0, e1;
+    ISO_CUDA(cudaEventCreate(&e0));
+    ISO_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+        ISO_CUDA(cudaEventRecord(e0, ctx->stream));
+        atomic_rate_kernel<<<grid, HIST_THREADS, smem, ctx->stream>>>(iters, bins, (unsigned int *)d_sink);
+        ISO_CUDA(cudaEventRecord(e1, ctx->stream));
+        ISO_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        ISO_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0 && ms < best) best = ms;  // the first launch warms up
+    }
+    ctx->launches += 4;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *updates_per_s = (double)grid * HIST_THREADS * iters * 4 / (best * 1e-3);
     return ISO_OK;
 }

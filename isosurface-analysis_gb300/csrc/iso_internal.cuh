@@ -44,6 +44,7 @@ void iso_clear_error();
 constexpr int ISO_MAX_BINS = 256;
 // LBVH surfaces are built and queried in groups of at most this many points
 // (default of iso_ctx_set_limit(ISO_LIMIT_LBVH_GROUP_POINTS))
+constexpr int64_t ISO_HIST_SEGMENT_VALUES = 0;  // fused kernel by default (faster at 256^3)
 constexpr int64_t ISO_LBVH_GROUP_POINTS = (int64_t)1 << 27;
 
 // ---------------------------------------------------------------------------
@@ -81,6 +82,7 @@ enum IsoBuf {
     BUF_STAGING_A,
     BUF_STAGING_B,
     BUF_CLNC,            // c*ln(c) for c < 65536, FP64
+    BUF_HIST_DUMP_SEG,   // per-pair global histograms of the segment-major schedule
     BUF_COUNT_
 };
 
@@ -100,6 +102,7 @@ struct iso_ctx {
     // admission hook: called by iso_ism once the surface counts fix the
     // request's device-memory need; a non-zero return aborts the request
     int64_t lbvh_group_points = ISO_LBVH_GROUP_POINTS;  // see iso_ctx_set_limit
+    int64_t hist_segment_values = ISO_HIST_SEGMENT_VALUES;  // 0: fused kernel for every length
     int (*admit)(void *user, size_t bytes) = nullptr;
     void *admit_user = nullptr;
     // request shape for the admission estimate (set by iso_ism)

@@ -107,6 +107,7 @@ def _load():
         "iso_server_destroy": (None, [P]),
         "iso_similarity_map_noalloc": (C.c_int, [P, C.c_int, C.c_int64, C.c_int64, C.c_int, P, P]),
         "iso_pair_map": (C.c_int, [P, P, C.c_int, C.c_int64, C.c_int64, C.c_int, P, C.c_int64, P]),
+        "iso_probe_counter_rate": (C.c_int, [P, C.c_int, C.POINTER(C.c_double)]),
         "iso_block_similarity": (C.c_int, [P, P, C.c_int64, C.c_int, P, C.c_int64, P]),
     }
     for name, (res, args) in sig.items():
@@ -178,6 +179,10 @@ class Context:
     def set_lbvh_group_points(self, points):
         _check(lib.iso_ctx_set_limit(self.handle, 1, int(points)))
 
+    def set_hist_segment_values(self, values):
+        """Fields longer than `values` use the segment-major histogram schedule (0: never)."""
+        _check(lib.iso_ctx_set_limit(self.handle, 2, int(values)))
+
     @property
     def launches(self):
         return int(lib.iso_ctx_launches(self.handle))
@@ -237,6 +242,12 @@ class Context:
         out = np.zeros((b.shape[0], 2), dtype=np.float32)
         _check(lib.iso_block_similarity(self.handle, _ptr(m), R, k, _ptr(b), b.shape[0], _ptr(out)))
         return out
+
+    def counter_rate(self, bins=256):
+        """Peak histogram counter updates per second (calibration kernel)."""
+        r = C.c_double()
+        _check(lib.iso_probe_counter_rate(self.handle, bins, C.byref(r)))
+        return r.value
 
     def copy_field(self, row, out):
         """Row `row` of the last ism() call's distance-field matrix into `out`."""

@@ -135,3 +135,101 @@ def test_counter_wraps(ctx, bins):
             want, _, _ = oracle.pair_histogram(f[i], f[j], bins)
             assert np.array_equal(joint[i, j], want), (i, j)
     assert np.abs(ism - oracle.similarity_map(f, bins, mode=0)).max() < TOL_F64
+
+
+# ---- segment-major schedule (fields longer than one 262144-value segment) ----
+
+SEG = 262144
+
+
+@pytest.fixture
+def seg_mode(ctx):
+    """The session context with the segment-major schedule for fields longer
+    than SEG values (off by default)."""
+    ctx.set_hist_segment_values(SEG)
+    yield
+    ctx.set_hist_segment_values(0)
+
+
+@pytest.mark.usefixtures("seg_mode")
+@pytest.mark.parametrize("n", [SEG + 1, 2 * SEG, 3 * SEG + 7])
+def test_segmented_bit_exact(ctx, n):
+    """Fields spanning several segments (a one-value last segment, an exact
+    multiple, a ragged tail): every segment's counts land in the pair's
+    histogram exactly once."""
+    f = fields_like_df(4, n, seed=n % 97)
+    ism, joint = ctx.similarity_map(f, 256, joint=True)
+    for i in range(4):
+        for j in range(4):
+            want, _, _ = oracle.pair_histogram(f[i], f[j], 256)
+            assert np.array_equal(joint[i, j], want), (i, j)
+    assert np.abs(ism - oracle.similarity_map(f, 256, mode=0)).max() < TOL_F64
+    assert np.array_equal(ism, ism.T)
+
+
+@pytest.mark.usefixtures("seg_mode")
+def test_segmented_wraps_in_both_halves(ctx):
+    """Constant fields put every value of a segment in one bin (four 16-bit
+    wraps per segment): the even bin (low half, carries into the high half),
+    the odd bin (high half, carry out of the word) and a word whose halves
+    both wrap."""
+    n = 4 * SEG + 3
+    bins = 2
+    rng = np.random.default_rng(5)
+    half = (rng.uniform(0, 1, n) < 0.5).astype(np.float32)
+    f = np.stack([np.zeros(n, np.float32), np.ones(n, np.float32), half, 1 - half])
+    f[0, 0] = 1.0   # give the constant fields a non-empty range
+    f[1, 0] = 0.0
+    ism, joint = ctx.similarity_map(f, bins, joint=True)
+    for i in range(4):
+        for j in range(4):
+            want, _, _ = oracle.pair_histogram(f[i], f[j], bins)
+            assert np.array_equal(joint[i, j], want), (i, j)
+    assert np.abs(ism - oracle.similarity_map(f, bins, mode=0)).max() < TOL_F64
+
+
+@pytest.mark.usefixtures("seg_mode")
+def test_segmented_cross_map_and_sums(ctx):
+    import isosim
+    n = 2 * SEG + 5
+    a = fields_like_df(3, n, seed=31)
+    b = fields_like_df(3, n, seed=32) * 1.5
+    cm = ctx.cross_map(a, b, 128)
+    fields = list(a) + list(b)
+    mins = [oracle.field_interval(x)[0] for x in fields]
+    maxs = [oracle.field_interval(x)[1] for x in fields]
+    sim, cols, rows = isosim.calculate_histogram_h(fields, mins, maxs, 128, multi=True)
+    assert np.abs(sim - cm).max() < TOL_F64
+    for i in range(3):
+        for j in range(3):
+            joint, cs, rs = oracle.pair_histogram(a[i], b[j], 128, (mins[i], maxs[i]), (mins[3 + j], maxs[3 + j]))
+            assert abs(cm[i, j] - oracle.mi_f64(joint, n)) < TOL_F64
+            assert np.array_equal(cols[i, j], cs) and np.array_equal(rows[i, j], rs)
+
+
+@pytest.mark.usefixtures("seg_mode")
+def test_segmented_matches_fused(ctx):
+    """The same pairs through the fused kernel (fields of one segment) and the
+    segment-major kernels (the fields repeated three times, so every bin count
+    triples): NMI is invariant under scaling all counts."""
+    f = fields_like_df(5, SEG // 2, seed=77)
+    fused = ctx.similarity_map(f, 256)
+    seg = ctx.similarity_map(np.concatenate([f, f, f], axis=1), 256)
+    assert np.abs(fused - seg).max() < TOL_F64
+
+
+def test_schedules_agree(ctx):
+    """The fused kernel (segmenting off) and the segment-major kernels at two
+    segment lengths give identical histograms and ISMs."""
+    f = fields_like_df(6, 3 * SEG + 11, seed=88)
+    try:
+        ctx.set_hist_segment_values(0)
+        ism0, j0 = ctx.similarity_map(f, 256, joint=True)
+        ctx.set_hist_segment_values(65536)
+        ism1, j1 = ctx.similarity_map(f, 256, joint=True)
+        ctx.set_hist_segment_values(SEG)
+        ism2, j2 = ctx.similarity_map(f, 256, joint=True)
+    finally:
+        ctx.set_hist_segment_values(0)
+    assert np.array_equal(j0, j1) and np.array_equal(j0, j2)
+    assert np.abs(ism0 - ism1).max() < TOL_F64 and np.abs(ism0 - ism2).max() < TOL_F64
