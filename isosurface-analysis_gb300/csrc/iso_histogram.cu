@@ -57,6 +57,8 @@ struct Binner {
     int mode;  // 0: fixed-point reciprocal with exact fallback, 1: exact division only, 2: step == 0
 };
 
+
+
 // Exact bucket of JointHistogram.cu:63-75 (IEEE division), clamped to [0, bins).
 __device__ __forceinline__ int exact_bucket(const Binner &b, float v) { return iso_bucket(v, b.mn, b.step, b.bins); }
 
@@ -91,11 +93,6 @@ __device__ __forceinline__ float2 fx_pair(float a, float b, float2 neg_mn, float
     return __ffma2_rn(__fadd2_rn(make_float2(a, b), neg_mn), r, make_float2(FX_BASE, FX_BASE));
 }
 
-__device__ __forceinline__ bool fx_ambiguous(uint32_t u) { return ((u & 0x1FFFu) == 0u) & (u != FX_BASE_BITS); }
-
-// bucket + (FX_BASE_BITS >> 13): the constant is folded into the bin offset
-__device__ __forceinline__ uint32_t fx_bucket_biased(uint32_t u, uint32_t lim) { return min(u >> FX_FRAC, lim); }
-
 // Bins (row = field-1 bucket, column = field-2 bucket) of the four voxels in x, y.
 template <int MODE>
 __device__ __forceinline__ void bins4(const Binner &bn, const float4 &x, const float4 &y, int &b0, int &b1, int &b2,
@@ -110,18 +107,24 @@ __device__ __forceinline__ void bins4(const Binner &bn, const float4 &x, const f
         const uint32_t ux2 = __float_as_uint(sx23.x), ux3 = __float_as_uint(sx23.y);
         const uint32_t uy0 = __float_as_uint(sy01.x), uy1 = __float_as_uint(sy01.y);
         const uint32_t uy2 = __float_as_uint(sy23.x), uy3 = __float_as_uint(sy23.y);
+        // bucket = min((u >> 13) - (bits(1536) >> 13), bins - 1) as unsigned:
+        // any input (also one outside the interval) stays inside the histogram
         const uint32_t kb = FX_BASE_BITS >> FX_FRAC;
-        const uint32_t lim = kb + (uint32_t)(bins - 1);
-        const uint32_t off = kb * (uint32_t)bins + kb;
-        // the outer clamp keeps any input (a value below the interval) inside
-        // the histogram; inside the interval it never acts
-        const uint32_t last = (uint32_t)(bins * bins - 1);
-        b0 = (int)min(fx_bucket_biased(ux0, lim) * (uint32_t)bins + fx_bucket_biased(uy0, lim) - off, last);
-        b1 = (int)min(fx_bucket_biased(ux1, lim) * (uint32_t)bins + fx_bucket_biased(uy1, lim) - off, last);
-        b2 = (int)min(fx_bucket_biased(ux2, lim) * (uint32_t)bins + fx_bucket_biased(uy2, lim) - off, last);
-        b3 = (int)min(fx_bucket_biased(ux3, lim) * (uint32_t)bins + fx_bucket_biased(uy3, lim) - off, last);
-        const bool slow = fx_ambiguous(ux0) | fx_ambiguous(ux1) | fx_ambiguous(ux2) | fx_ambiguous(ux3) |
-                          fx_ambiguous(uy0) | fx_ambiguous(uy1) | fx_ambiguous(uy2) | fx_ambiguous(uy3);
+        const uint32_t top = (uint32_t)(bins - 1);
+        b0 = (int)(min((ux0 >> FX_FRAC) - kb, top) * (uint32_t)bins + min((uy0 >> FX_FRAC) - kb, top));
+        b1 = (int)(min((ux1 >> FX_FRAC) - kb, top) * (uint32_t)bins + min((uy1 >> FX_FRAC) - kb, top));
+        b2 = (int)(min((ux2 >> FX_FRAC) - kb, top) * (uint32_t)bins + min((uy2 >> FX_FRAC) - kb, top));
+        b3 = (int)(min((ux3 >> FX_FRAC) - kb, top) * (uint32_t)bins + min((uy3 >> FX_FRAC) - kb, top));
+        // Ambiguous values: u = bits(1536) | w with w a nonzero multiple of
+        // 2^13, i.e. the lowest set bit of u lies in bits 13..21 (for w = 0
+        // the lowest set bit is bit 22 of bits(1536)).  u & (2^29 - u) keeps
+        // that lowest bit (2^29 - u equals -u below bit 29) and adds bit 29 for
+        // a NaN (exponent bits all set), which in-range values never have.  One
+        // OR over the eight values tests them all; both kinds take the division.
+        constexpr uint32_t B29 = 0x20000000u;
+        const uint32_t low = (ux0 & (B29 - ux0)) | (ux1 & (B29 - ux1)) | (ux2 & (B29 - ux2)) | (ux3 & (B29 - ux3)) |
+                             (uy0 & (B29 - uy0)) | (uy1 & (B29 - uy1)) | (uy2 & (B29 - uy2)) | (uy3 & (B29 - uy3));
+        const bool slow = (low & 0x203FE000u) != 0u;
         if (__builtin_expect(slow, 0)) {
             const int4 e = exact_bins4(bn.mn, bn.step, bins, x, y);
             b0 = e.x;
@@ -137,8 +140,8 @@ __device__ __forceinline__ void bins4(const Binner &bn, const float4 &x, const f
     }
 }
 
-// Counts one bin as a 16-bit half of a shared 32-bit word.  The returned old
-// word tells this thread exactly when a half wraps: the low half's 16 bits
+// A bin is counted as a 16-bit half of a shared 32-bit word.  The old word an
+// atomic returns tells its thread exactly when a half wraps: the low half's 16 bits
 // advance only by its own increments, the high half's by its increments plus
 // the low half's carries.  Wraps are logged as corrections:
 //   low half wraps  -> low bin +65536, high bin -1 (the carry it received)
@@ -163,16 +166,35 @@ __device__ __noinline__ void log_wrap(int bin, uint32_t sh, uint32_t old, int4 *
     }
 }
 
-__device__ __forceinline__ void count_bin(uint32_t *words, int bin, int4 *ev, int cap, unsigned int *nev, int *error)
+// Counts four bins.  A bin is a 16-bit half of word bin/2 (odd bins in the
+// high half).  old * (odd ? 1 : 65536) moves the counted half of the old word
+// to the top 16 bits, so the half wrapped exactly when that product is
+// >= 0xFFFF0000; one test covers the four updates, and the rare wraps go to
+// wrap(bin, odd, old).
+template <class Wrap>
+__device__ __forceinline__ void count4(uint32_t *words, int b0, int b1, int b2, int b3, const Wrap &wrap)
 {
-    // odd bins live in the high half: increment 0x10000 and wrap mask
-    // 0xFFFF0000, even bins 1 and 0xFFFF (integer multiply-adds instead of
-    // shifts keep the ALU pipe free)
+    const uint32_t o0 = (uint32_t)b0 & 1u, o1 = (uint32_t)b1 & 1u, o2 = (uint32_t)b2 & 1u, o3 = (uint32_t)b3 & 1u;
+    const uint32_t old0 = atomicAdd(&words[b0 >> 1], o0 * 0xFFFFu + 1u);
+    const uint32_t old1 = atomicAdd(&words[b1 >> 1], o1 * 0xFFFFu + 1u);
+    const uint32_t old2 = atomicAdd(&words[b2 >> 1], o2 * 0xFFFFu + 1u);
+    const uint32_t old3 = atomicAdd(&words[b3 >> 1], o3 * 0xFFFFu + 1u);
+    const uint32_t t0 = old0 * (65536u - o0 * 65535u), t1 = old1 * (65536u - o1 * 65535u);
+    const uint32_t t2 = old2 * (65536u - o2 * 65535u), t3 = old3 * (65536u - o3 * 65535u);
+    if (__builtin_expect(max(max(t0, t1), max(t2, t3)) >= 0xFFFF0000u, 0)) {
+        if (t0 >= 0xFFFF0000u) wrap(b0, o0, old0);
+        if (t1 >= 0xFFFF0000u) wrap(b1, o1, old1);
+        if (t2 >= 0xFFFF0000u) wrap(b2, o2, old2);
+        if (t3 >= 0xFFFF0000u) wrap(b3, o3, old3);
+    }
+}
+
+template <class Wrap>
+__device__ __forceinline__ void count1(uint32_t *words, int bin, const Wrap &wrap)
+{
     const uint32_t odd = (uint32_t)bin & 1u;
-    const uint32_t inc = odd * 0xFFFFu + 1u;
-    const uint32_t mask = inc * 0xFFFFu;
-    const uint32_t old = atomicAdd(&words[bin >> 1], inc);
-    if (__builtin_expect((old & mask) == mask, 0)) log_wrap(bin, odd << 4, old, ev, cap, nev, error);
+    const uint32_t old = atomicAdd(&words[bin >> 1], odd * 0xFFFFu + 1u);
+    if (old * (65536u - odd * 65535u) >= 0xFFFF0000u) wrap(bin, odd, old);
 }
 
 __device__ __forceinline__ double clnc_of(const double *table, unsigned long long c)
@@ -183,7 +205,7 @@ __device__ __forceinline__ double clnc_of(const double *table, unsigned long lon
 }
 
 // Streams values [v0, v1) of one field pair (v0 a multiple of 4, rows 16-byte
-// aligned) into count(bin).  Two load pairs alternate so that one is in
+// aligned) into the shared histogram count.words (wraps to count.wrap).  Two load pairs alternate so that one is in
 // flight while the other is binned.
 template <int MODE, class Count>
 __device__ __forceinline__ void stream_values(const Binner &bn, const float *f1, const float *f2, int64_t v0,
@@ -207,10 +229,7 @@ __device__ __forceinline__ void stream_values(const Binner &bn, const float *f1,
         }
         int c0, c1, c2, c3;
         bins4<MODE>(bn, xa, ya, c0, c1, c2, c3);
-        count(c0);
-        count(c1);
-        count(c2);
-        count(c3);
+        count4(count.words, c0, c1, c2, c3, count.wrap);
         if (qb >= n4) break;
         const int qa = qb + step;
         if (qa < n4) {
@@ -218,25 +237,31 @@ __device__ __forceinline__ void stream_values(const Binner &bn, const float *f1,
             ya = __ldg(p2 + qa);
         }
         bins4<MODE>(bn, xb, yb, c0, c1, c2, c3);
-        count(c0);
-        count(c1);
-        count(c2);
-        count(c3);
+        count4(count.words, c0, c1, c2, c3, count.wrap);
         q = qa;
     }
     for (int64_t v = v0 + ((int64_t)n4 << 2) + threadIdx.x; v < v1; v += blockDim.x) {
         const int bin = bn.mode == 2 ? 0 : exact_bucket(bn, f1[v]) * bn.bins + exact_bucket(bn, f2[v]);
-        count(bin);
+        count1(count.words, bin, count.wrap);
     }
 }
 
-struct EventCount {
-    uint32_t *words;
+// Wraps logged as per-CTA events (fused kernel).
+struct EventWrap {
     int4 *ev;
     int cap;
     unsigned int *nev;
     int *error;
-    __device__ __forceinline__ void operator()(int bin) const { count_bin(words, bin, ev, cap, nev, error); }
+    __device__ __forceinline__ void operator()(int bin, uint32_t odd, uint32_t old) const
+    {
+        log_wrap(bin, odd << 4, old, ev, cap, nev, error);
+    }
+};
+
+template <class Wrap>
+struct Counter {
+    uint32_t *words;
+    Wrap wrap;
 };
 
 // Interval of one pair: the union of both fields' intervals; step, reciprocal
@@ -264,8 +289,8 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
     __shared__ int s_task;
     __shared__ unsigned int s_nev;
     __shared__ double s_red[3][HIST_THREADS / 32];
-    __shared__ unsigned long long s_colsum[ISO_MAX_BINS];
-    __shared__ unsigned long long s_rowsum[ISO_MAX_BINS];
+    __shared__ uint32_t s_colsum[ISO_MAX_BINS];  // marginals (n < 2^32)
+    __shared__ uint32_t s_rowsum[ISO_MAX_BINS];
 
     const int bins = a.bins;
     const int nwords = bins * bins / 2;
@@ -296,7 +321,7 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
         const float *f2 = a.fb + (size_t)j * a.stride;
 
         // streaming loop, one load pair in flight ahead of the one being binned
-        const EventCount cnt{words, ev, a.event_cap, &s_nev, a.error};
+        const Counter<EventWrap> cnt{words, EventWrap{ev, a.event_cap, &s_nev, a.error}};
         if (bn.mode == 0) stream_values<0>(bn, f1, f2, 0, a.n, cnt);
         else stream_values<1>(bn, f1, f2, 0, a.n, cnt);
         __syncthreads();
@@ -322,43 +347,54 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
             const uint32_t c16 = (words[bin >> 1] >> ((bin & 1) << 4)) & 0xffffu;
             const unsigned long long ctrue = (unsigned long long)((long long)c16 + corr);
             hxy -= clnc_of(a.clnc, ctrue) - clnc_of(a.clnc, c16);
-            atomicAdd(&s_rowsum[bin / bins], (unsigned long long)corr);
-            atomicAdd(&s_colsum[bin % bins], (unsigned long long)corr);
+            atomicAdd(&s_rowsum[bin / bins], (uint32_t)corr);  // modular: corr may be negative
+            atomicAdd(&s_colsum[bin % bins], (uint32_t)corr);
             ev[e].z = (int)c16;
             ev[e].w = (int)ctrue;  // only read back for histogram dumps
         }
         __syncthreads();  // the bin pass below clears the words read above
 
         // ---- bin pass: 16-bit counts, marginals, sum(c ln c); clears the bins.
-        // Thread (g, w) reads word column w of rows g, g+groups, ...
+        // Thread (g, w) reads word column w of rows g, g+groups, ...  With a
+        // multiple of 32 words per row a warp covers part of one row, and a
+        // warp sum replaces the per-thread row-sum atomics.
         const bool dump = a.joint_dump != nullptr;
         {
             const int groups = blockDim.x / wpr;
             const int w = threadIdx.x % wpr, g = threadIdx.x / wpr;
+            const bool warp_rows = (wpr & 31) == 0;
             if (g < groups) {
                 uint32_t cs0 = 0, cs1 = 0;
                 for (int r = g; r < bins; r += groups) {
                     const uint32_t word = words[r * wpr + w];
-                    if (!word && !dump) continue;
-                    words[r * wpr + w] = 0;
-                    const uint32_t c0 = word & 0xffffu, c1 = word >> 16;
-                    cs0 += c0;
-                    cs1 += c1;
-                    atomicAdd(&s_rowsum[r], (unsigned long long)(c0 + c1));
-                    if (c0) hxy -= __ldg(a.clnc + c0);
-                    if (c1) hxy -= __ldg(a.clnc + c1);
-                    if (dump) {
-                        const int c = 2 * w;
-                        a.joint_dump[(((size_t)i * a.m + j) * bins + r) * bins + c] = c0;
-                        a.joint_dump[(((size_t)i * a.m + j) * bins + r) * bins + c + 1] = c1;
-                        if (a.symmetric && i != j) {
-                            a.joint_dump[(((size_t)j * a.m + i) * bins + c) * bins + r] = c0;
-                            a.joint_dump[(((size_t)j * a.m + i) * bins + c + 1) * bins + r] = c1;
+                    uint32_t c0 = 0, c1 = 0;
+                    if (word || dump) {
+                        words[r * wpr + w] = 0;
+                        c0 = word & 0xffffu;
+                        c1 = word >> 16;
+                        cs0 += c0;
+                        cs1 += c1;
+                        if (c0) hxy -= __ldg(a.clnc + c0);
+                        if (c1) hxy -= __ldg(a.clnc + c1);
+                        if (dump) {
+                            const int c = 2 * w;
+                            a.joint_dump[(((size_t)i * a.m + j) * bins + r) * bins + c] = c0;
+                            a.joint_dump[(((size_t)i * a.m + j) * bins + r) * bins + c + 1] = c1;
+                            if (a.symmetric && i != j) {
+                                a.joint_dump[(((size_t)j * a.m + i) * bins + c) * bins + r] = c0;
+                                a.joint_dump[(((size_t)j * a.m + i) * bins + c + 1) * bins + r] = c1;
+                            }
                         }
                     }
+                    if (warp_rows) {
+                        const uint32_t rs = __reduce_add_sync(0xffffffffu, c0 + c1);
+                        if (lane == 0 && rs) atomicAdd(&s_rowsum[r], rs);
+                    } else if (c0 + c1) {
+                        atomicAdd(&s_rowsum[r], c0 + c1);
+                    }
                 }
-                if (cs0) atomicAdd(&s_colsum[2 * w], (unsigned long long)cs0);
-                if (cs1) atomicAdd(&s_colsum[2 * w + 1], (unsigned long long)cs1);
+                if (cs0) atomicAdd(&s_colsum[2 * w], cs0);
+                if (cs1) atomicAdd(&s_colsum[2 * w + 1], cs1);
             }
         }
         __syncthreads();
@@ -381,7 +417,7 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
         }
         double hx = 0.0, hy = 0.0;
         for (int c = threadIdx.x; c < bins; c += blockDim.x) {
-            const unsigned long long cs = s_colsum[c], rs = s_rowsum[c];
+            const unsigned long long cs = s_colsum[c], rs = s_rowsum[c];  // exact: true sums < 2^32
             if (cs) hx -= clnc_of(a.clnc, cs);
             if (rs) hy -= clnc_of(a.clnc, rs);
             if (a.colrow_dump) {
@@ -454,7 +490,7 @@ struct SegArgs {
     unsigned int *counter;
 };
 
-// Wrap corrections straight into the pair's global histogram (see count_bin).
+// Wrap corrections straight into the pair's global histogram (see count4).
 __device__ __noinline__ void log_wrap_global(uint32_t *gh, int bin, uint32_t odd, uint32_t old)
 {
     const int lo = bin & ~1, hi = bin | 1;
@@ -467,19 +503,13 @@ __device__ __noinline__ void log_wrap_global(uint32_t *gh, int bin, uint32_t odd
     }
 }
 
-__device__ __forceinline__ void count_bin_global(uint32_t *words, int bin, uint32_t *gh)
-{
-    const uint32_t odd = (uint32_t)bin & 1u;
-    const uint32_t inc = odd * 0xFFFFu + 1u;
-    const uint32_t mask = inc * 0xFFFFu;
-    const uint32_t old = atomicAdd(&words[bin >> 1], inc);
-    if (__builtin_expect((old & mask) == mask, 0)) log_wrap_global(gh, bin, odd, old);
-}
-
-struct GlobalCount {
-    uint32_t *words;
+// Wraps corrected straight in the pair's global histogram (segment-major kernel).
+struct GlobalWrap {
     uint32_t *gh;
-    __device__ __forceinline__ void operator()(int bin) const { count_bin_global(words, bin, gh); }
+    __device__ __forceinline__ void operator()(int bin, uint32_t odd, uint32_t old) const
+    {
+        log_wrap_global(gh, bin, odd, old);
+    }
 };
 
 __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_seg_kernel(SegArgs a)
@@ -519,7 +549,7 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_seg_kernel(Se
         const int64_t v1 = v0 + a.seg_len < a.n ? v0 + a.seg_len : a.n;
         const float *f1 = a.fa + (size_t)i * a.stride;
         const float *f2 = a.fb + (size_t)j * a.stride;
-        const GlobalCount cnt{words, gh};
+        const Counter<GlobalWrap> cnt{words, GlobalWrap{gh}};
         if (bn.mode == 0) stream_values<0>(bn, f1, f2, v0, v1, cnt);
         else stream_values<1>(bn, f1, f2, v0, v1, cnt);
         __syncthreads();
@@ -549,7 +579,7 @@ struct MiArgs {
 // One block per pair: marginals and sum(c ln c) of the global histogram, NMI.
 __global__ void __launch_bounds__(256) joint_mi_kernel(MiArgs a)
 {
-    __shared__ unsigned long long s_row[ISO_MAX_BINS], s_col[ISO_MAX_BINS];
+    __shared__ uint32_t s_row[ISO_MAX_BINS], s_col[ISO_MAX_BINS];  // n < 2^32
     __shared__ double s_red[3][8];
     const int p = blockIdx.x;
     const int2 task = a.tasks[p];
@@ -572,8 +602,8 @@ __global__ void __launch_bounds__(256) joint_mi_kernel(MiArgs a)
         }
         if (!c) continue;
         hxy -= clnc_of(a.clnc, c);
-        atomicAdd(&s_row[r], (unsigned long long)c);
-        atomicAdd(&s_col[col], (unsigned long long)c);
+        atomicAdd(&s_row[r], c);
+        atomicAdd(&s_col[col], c);
     }
     __syncthreads();
     double hx = 0.0, hy = 0.0;
@@ -739,6 +769,7 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
 {
     if (num_tasks_in <= 0) return ISO_OK;
     if (num_tasks_in > 0x7fffffff) return iso_fail(ISO_ERR_ARG, "too many pair tasks");
+    if (n > (int64_t)0xffffffff) return iso_fail(ISO_ERR_ARG, "fields longer than 2^32 - 1 values");
     if (bins < 2 || bins > ISO_MAX_BINS || (bins & 1))
         return iso_fail(ISO_ERR_ARG, "bins must be even and in [2, %d], got %d", ISO_MAX_BINS, bins);
     if (stride % 4 != 0 || ((uintptr_t)d_fields_a & 15) || ((uintptr_t)d_fields_b & 15))

@@ -119,3 +119,28 @@ def test_every_value_stays_inside_the_histogram():
     v = np.array([mx, np.nextafter(mx, np.float32(9)), mx * 1.001], np.float32)
     fx, _ = fixed_point_bucket(v, mn, step, bins)
     assert fx.min() >= 0 and fx.max() <= bins - 1
+
+
+def test_lowest_set_bit_form_of_the_ambiguity_test():
+    """The kernels test 'w is a nonzero multiple of 2^13' (u = bits(1536) | w)
+    as 'the lowest set bit of u lies in bits 13..21' so that eight values
+    combine with one OR; exhaustive over every u of the fixed-point range."""
+    u = (BASE_BITS + np.arange(1 << 22, dtype=np.int64)).astype(np.uint32)
+    direct = ((u & 0x1FFF) == 0) & (u != BASE_BITS)
+    low = u & (np.uint32(0) - u)
+    assert np.array_equal((low & np.uint32(0x3FE000)) != 0, direct)
+
+
+def test_multiply_high_forms():
+    """x >> 13 == umulhi(x, 2^19) and x >> 1 == umulhi(x, 2^31); the counted
+    half of a word wraps exactly when old * (65536 - odd * 65535) >= 0xFFFF0000."""
+    rng = np.random.default_rng(4)
+    x = rng.integers(0, 1 << 32, 100000, dtype=np.uint64)
+    assert np.array_equal((x * (1 << 19)) >> 32, x >> 13)
+    assert np.array_equal((x * (1 << 31)) >> 32, x >> 1)
+    old = np.concatenate([x, [0xFFFF, 0xFFFF0000, 0x1234FFFF, 0xFFFF1234, 0xFFFFFFFF, 0]]).astype(np.uint64)
+    for odd in (0, 1):
+        sh = 65536 - odd * 65535
+        t = (old * sh) & 0xFFFFFFFF
+        half = (old >> (16 * odd)) & 0xFFFF
+        assert np.array_equal(t >= 0xFFFF0000, half == 0xFFFF)

@@ -233,3 +233,21 @@ def test_schedules_agree(ctx):
         ctx.set_hist_segment_values(0)
     assert np.array_equal(j0, j1) and np.array_equal(j0, j2)
     assert np.abs(ism0 - ism1).max() < TOL_F64 and np.abs(ism0 - ism2).max() < TOL_F64
+
+
+def test_nan_values_take_bucket_zero(ctx):
+    """NaN never enters a field interval (the comparisons in getInterval fail)
+    and converts to bucket 0 in the reference's GPU kernel ((int)NaN is 0 on
+    the device); the fixed-point path hands NaN values to the division."""
+    f = fields_like_df(3, 100003, seed=5)
+    f[0, ::997] = np.nan
+    f[2, 5::1231] = np.nan
+    ism, joint = ctx.similarity_map(f, 64, joint=True)
+    iv = [oracle.field_interval(x) for x in f]
+    for i in range(3):
+        for j in range(3):
+            lo = min(iv[i][0], iv[j][0])
+            a = np.where(np.isnan(f[i]), lo, f[i]).astype(np.float32)
+            b = np.where(np.isnan(f[j]), lo, f[j]).astype(np.float32)
+            want, _, _ = oracle.pair_histogram(a, b, 64, iv[i], iv[j])
+            assert np.array_equal(joint[i, j], want), (i, j)
