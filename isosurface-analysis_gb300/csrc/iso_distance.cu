@@ -279,8 +279,7 @@ __device__ __forceinline__ float max3f(float a, float b, float c)
 
 // Sample point prepared for packed box tests.
 struct Query {
-    float2 sx, sy, sz;     // (s, s) per axis
-    float2 nsx, nsy, nsz;  // (-s, -s)
+    float2 sx, sy, sz;  // (s, s) per axis
 };
 
 __device__ __forceinline__ Query make_query(float3 s)
@@ -289,9 +288,6 @@ __device__ __forceinline__ Query make_query(float3 s)
     q.sx = make_float2(s.x, s.x);
     q.sy = make_float2(s.y, s.y);
     q.sz = make_float2(s.z, s.z);
-    q.nsx = make_float2(-s.x, -s.x);
-    q.nsy = make_float2(-s.y, -s.y);
-    q.nsz = make_float2(-s.z, -s.z);
     return q;
 }
 
@@ -301,9 +297,11 @@ __device__ __forceinline__ Query make_query(float3 s)
 // exactly its canonical distance.
 __device__ __forceinline__ float2 child_dist2(const Query &q, const float4 &a, const float4 &b, const float4 &c)
 {
-    const float2 ux = __fadd2_rn(make_float2(a.x, a.y), q.nsx), vx = __fadd2_rn(q.sx, make_float2(b.z, b.w));
-    const float2 uy = __fadd2_rn(make_float2(a.z, a.w), q.nsy), vy = __fadd2_rn(q.sy, make_float2(c.x, c.y));
-    const float2 uz = __fadd2_rn(make_float2(b.x, b.y), q.nsz), vz = __fadd2_rn(q.sz, make_float2(c.z, c.w));
+    // lo - s as fma(s, -1, lo): one rounding of the exact difference
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    const float2 ux = __ffma2_rn(q.sx, m1, make_float2(a.x, a.y)), vx = __fadd2_rn(q.sx, make_float2(b.z, b.w));
+    const float2 uy = __ffma2_rn(q.sy, m1, make_float2(a.z, a.w)), vy = __fadd2_rn(q.sy, make_float2(c.x, c.y));
+    const float2 uz = __ffma2_rn(q.sz, m1, make_float2(b.x, b.y)), vz = __fadd2_rn(q.sz, make_float2(c.z, c.w));
     const float2 gx = make_float2(max3f(ux.x, vx.x, 0.0f), max3f(ux.y, vx.y, 0.0f));
     const float2 gy = make_float2(max3f(uy.x, vy.x, 0.0f), max3f(uy.y, vy.y, 0.0f));
     const float2 gz = make_float2(max3f(uz.x, vz.x, 0.0f), max3f(uz.y, vz.y, 0.0f));
@@ -311,11 +309,13 @@ __device__ __forceinline__ float2 child_dist2(const Query &q, const float4 &a, c
 }
 
 // Query layout: a warp owns an 8 (z) x 4 (y) patch of sample columns and each
-// thread sweeps RUN_X consecutive samples along x.  A block stacks four warps
-// in y, covering 16 (y) x 8 (z) x RUN_X (x) samples.  The nearest point of one
-// sample seeds the next sample's bound (its canonical distance to that real
-// point), which keeps the traversal exact and prunes almost everything but
-// the nearest region.
+// thread sweeps RUN_X consecutive samples along x, two at a time (x, x+1):
+// one node load serves both samples of a lane, which halves the L1 traffic
+// per sample (the broadcast node loads' register writeback is what bounds
+// the query kernel).  A block stacks four warps in y, covering 16 (y) x 8 (z)
+// x RUN_X (x) samples.  The nearest points of one pair seed the next pair's
+// bounds (canonical distances to those real points), which keeps the
+// traversal exact and prunes almost everything but the nearest region.
 constexpr int PATCH_Z = 8, PATCH_Y = 4, WARPS_Y = QUERY_THREADS / 32, RUN_X = 8;
 
 __device__ __forceinline__ void load_node(const BvhNode *nodes, int cur, float4 &a, float4 &b, float4 &c, int4 &d)
@@ -326,54 +326,64 @@ __device__ __forceinline__ void load_node(const BvhNode *nodes, int cur, float4 
     d = __ldg(&nodes[cur].d);
 }
 
-// Exact nearest canonical squared distance for the 32 samples of a warp,
-// traversed as one packet: every lane evaluates every visited node against its
-// own sample and bound, and a subtree is skipped only when no lane's bound
-// admits it (bounds only decrease, so skipping is safe for every lane).  Node
-// addresses are warp-uniform (one broadcast load per node) and no lane idles.
-// `best` starts as the canonical distance to a real point bp; returns the
-// minimum, bp its point.
-__device__ __forceinline__ float traverse_packet(const BvhNode *nodes, const Query &q, float best, float3 &bp,
-                                                 int *error)
+// Exact nearest canonical squared distances for the 64 samples of a warp (two
+// per lane, A and B), traversed as one packet: every lane evaluates every
+// visited node against both its samples and bounds, and a subtree is skipped
+// only when no sample's bound admits it (bounds only decrease, so skipping is
+// safe for every sample).  Node addresses are warp-uniform (one broadcast
+// load per node) and no lane idles.  Each best starts as the canonical
+// distance to a real point bp; on return it is the minimum and bp its point.
+__device__ __forceinline__ void traverse_packet2(const BvhNode *nodes, const Query &qa, const Query &qb, float &best_a,
+                                                 float3 &bp_a, float &best_b, float3 &bp_b, int *error)
 {
     int stack[STACK_DEPTH];     // warp-uniform node ids
-    float sdist[STACK_DEPTH];   // this lane's distance to each postponed node
+    float sda[STACK_DEPTH];     // sample A's distance to each postponed node
+    float sdb[STACK_DEPTH];     // sample B's
     int top = 0;
     int cur = 0;
     for (;;) {
         float4 a, b, c;
         int4 d;
         load_node(nodes, cur, a, b, c, d);
-        const float2 dd = child_dist2(q, a, b, c);
+        const float2 da = child_dist2(qa, a, b, c);
+        const float2 db = child_dist2(qb, a, b, c);
         const int left = d.x, right = d.y;
-        const float dl = dd.x, dr = dd.y;
         bool gl = false, gr = false;
         if (left & LEAF_BIT) {
-            if (dl < best) {
-                best = dl;
-                bp = make_float3(a.x, a.z, b.x);
+            if (da.x < best_a) {
+                best_a = da.x;
+                bp_a = make_float3(a.x, a.z, b.x);
+            }
+            if (db.x < best_b) {
+                best_b = db.x;
+                bp_b = make_float3(a.x, a.z, b.x);
             }
         } else {
-            gl = dl < best;
+            gl = (da.x < best_a) | (db.x < best_b);
         }
         if (right & LEAF_BIT) {
-            if (dr < best) {
-                best = dr;
-                bp = make_float3(a.y, a.w, b.y);
+            if (da.y < best_a) {
+                best_a = da.y;
+                bp_a = make_float3(a.y, a.w, b.y);
+            }
+            if (db.y < best_b) {
+                best_b = db.y;
+                bp_b = make_float3(a.y, a.w, b.y);
             }
         } else {
-            gr = dr < best;
+            gr = (da.y < best_a) | (db.y < best_b);
         }
         const bool any_l = __any_sync(0xffffffffu, gl), any_r = __any_sync(0xffffffffu, gr);
         if (any_l && any_r) {
-            // most lanes' nearer child first
-            const bool lfirst = __popc(__ballot_sync(0xffffffffu, dl <= dr)) >= 16;
+            // most lanes' nearer child (for sample A) first
+            const bool lfirst = __popc(__ballot_sync(0xffffffffu, da.x <= da.y)) >= 16;
             if (top == STACK_DEPTH) {
                 atomicExch(error, 2);
                 break;
             }
             stack[top] = lfirst ? right : left;
-            sdist[top] = lfirst ? dr : dl;
+            sda[top] = lfirst ? da.y : da.x;
+            sdb[top] = lfirst ? db.y : db.x;
             ++top;
             cur = lfirst ? left : right;
         } else if (any_l) {
@@ -381,12 +391,11 @@ __device__ __forceinline__ float traverse_packet(const BvhNode *nodes, const Que
         } else if (any_r) {
             cur = right;
         } else {
-            while (top > 0 && !__any_sync(0xffffffffu, sdist[top - 1] < best)) --top;
+            while (top > 0 && !__any_sync(0xffffffffu, (sda[top - 1] < best_a) | (sdb[top - 1] < best_b))) --top;
             if (top == 0) break;
             cur = stack[--top];
         }
     }
-    return best;
 }
 
 __global__ void __launch_bounds__(QUERY_THREADS) bvh_query_kernel(Bvh b, SampleGrid g, float *fields, int64_t stride)
@@ -454,18 +463,40 @@ __global__ void __launch_bounds__(QUERY_THREADS) bvh_query_kernel(Bvh b, SampleG
     }
     // every lane runs every step (the packet traversal needs the whole warp);
     // lanes past the grid edge repeat a valid sample and do not store
-    for (int k = 0; k < RUN_X; ++k) {
-        const int64_t x = x0 + k;
-        if (!__any_sync(0xffffffffu, col_valid && x < X10)) break;
-        const bool valid = col_valid && x < X10;
-        const int64_t idx = ((x < X10 ? x : X10 - 1) * g.Y10 + yc) * g.Z10 + zc;
+    float3 bq = bp;  // nearest point of the previous pair's second sample
+    for (int k = 0; k < RUN_X; k += 2) {
+        const int64_t xa = x0 + k, xb = x0 + k + 1;
+        if (!__any_sync(0xffffffffu, col_valid && xa < X10)) break;
+        const bool va = col_valid && xa < X10, vb = col_valid && xb < X10;
+        const int64_t ia = ((xa < X10 ? xa : X10 - 1) * g.Y10 + yc) * g.Z10 + zc;
+        const int64_t ib = ((xb < X10 ? xb : X10 - 1) * g.Y10 + yc) * g.Z10 + zc;
+        const float3 sa = k == 0 ? sp : sample_point(g, ia);
+        const float3 sb = sample_point(g, ib);
+        // bounds: the nearer of the previous pair's two nearest points (for
+        // the first pair, the greedy candidate of sample A)
+        float best_a = k == 0 ? best : iso_dist2(__fsub_rn(sa.x, bq.x), __fsub_rn(sa.y, bq.y), __fsub_rn(sa.z, bq.z));
+        float3 bp_a = k == 0 ? bp : bq;
         if (k > 0) {
-            sp = sample_point(g, idx);
-            qy = make_query(sp);
-            best = iso_dist2(__fsub_rn(sp.x, bp.x), __fsub_rn(sp.y, bp.y), __fsub_rn(sp.z, bp.z));
+            const float alt = iso_dist2(__fsub_rn(sa.x, bp.x), __fsub_rn(sa.y, bp.y), __fsub_rn(sa.z, bp.z));
+            if (alt < best_a) {
+                best_a = alt;
+                bp_a = bp;
+            }
         }
-        best = traverse_packet(nodes, qy, best, bp, b.error);
-        if (valid) out[idx] = __fsqrt_rn(best);
+        float best_b = iso_dist2(__fsub_rn(sb.x, bq.x), __fsub_rn(sb.y, bq.y), __fsub_rn(sb.z, bq.z));
+        float3 bp_b = bq;
+        {
+            const float alt = iso_dist2(__fsub_rn(sb.x, bp.x), __fsub_rn(sb.y, bp.y), __fsub_rn(sb.z, bp.z));
+            if (alt < best_b) {
+                best_b = alt;
+                bp_b = bp;
+            }
+        }
+        traverse_packet2(nodes, make_query(sa), make_query(sb), best_a, bp_a, best_b, bp_b, b.error);
+        if (va) out[ia] = __fsqrt_rn(best_a);
+        if (vb) out[ib] = __fsqrt_rn(best_b);
+        bp = bp_a;
+        bq = bp_b;
     }
 }
 
