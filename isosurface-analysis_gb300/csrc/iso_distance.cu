@@ -464,28 +464,50 @@ __global__ void __launch_bounds__(QUERY_THREADS) bvh_query_kernel(Bvh b, SampleG
     // every lane runs every step (the packet traversal needs the whole warp);
     // lanes past the grid edge repeat a valid sample and do not store
     float3 bq = bp;  // nearest point of the previous pair's second sample
+    // y and z coordinates are fixed per lane (the sample-grid formula of
+    // BVH.cu:393-406, as sample_point computes it)
+    const float sy = __fdiv_rn((float)(yc * g.ds + g.ds / 2), (float)g.Y);
+    const float sz = __fdiv_rn((float)(zc * g.ds + g.ds / 2), (float)g.Z);
     for (int k = 0; k < RUN_X; k += 2) {
         const int64_t xa = x0 + k, xb = x0 + k + 1;
         if (!__any_sync(0xffffffffu, col_valid && xa < X10)) break;
         const bool va = col_valid && xa < X10, vb = col_valid && xb < X10;
-        const int64_t ia = ((xa < X10 ? xa : X10 - 1) * g.Y10 + yc) * g.Z10 + zc;
-        const int64_t ib = ((xb < X10 ? xb : X10 - 1) * g.Y10 + yc) * g.Z10 + zc;
-        const float3 sa = k == 0 ? sp : sample_point(g, ia);
-        const float3 sb = sample_point(g, ib);
-        // bounds: the nearer of the previous pair's two nearest points (for
-        // the first pair, the greedy candidate of sample A)
+        const int64_t xac = xa < X10 ? xa : X10 - 1, xbc = xb < X10 ? xb : X10 - 1;
+        const int64_t ia = (xac * g.Y10 + yc) * g.Z10 + zc;
+        const int64_t ib = (xbc * g.Y10 + yc) * g.Z10 + zc;
+        const float3 sa = make_float3(__fdiv_rn((float)(xac * g.ds + g.ds / 2), (float)g.X), sy, sz);
+        const float3 sb = make_float3(__fdiv_rn((float)(xbc * g.ds + g.ds / 2), (float)g.X), sy, sz);
+        // bounds: the nearest of the previous pair's nearest points, this
+        // lane's and its z and y neighbours' (for the first pair, the greedy
+        // candidate of sample A)
         float best_a = k == 0 ? best : iso_dist2(__fsub_rn(sa.x, bq.x), __fsub_rn(sa.y, bq.y), __fsub_rn(sa.z, bq.z));
         float3 bp_a = k == 0 ? bp : bq;
-        if (k > 0) {
-            const float alt = iso_dist2(__fsub_rn(sa.x, bp.x), __fsub_rn(sa.y, bp.y), __fsub_rn(sa.z, bp.z));
-            if (alt < best_a) {
-                best_a = alt;
-                bp_a = bp;
-            }
-        }
         float best_b = iso_dist2(__fsub_rn(sb.x, bq.x), __fsub_rn(sb.y, bq.y), __fsub_rn(sb.z, bq.z));
         float3 bp_b = bq;
-        {
+        if (k > 0) {
+#pragma unroll
+            for (int o = 0; o < 3; ++o) {
+                const int mask = o == 0 ? 0 : (o == 1 ? 1 : PATCH_Z);
+                float3 cnd;
+                if (o == 0) {
+                    cnd = bp;
+                } else {
+                    cnd.x = __shfl_xor_sync(0xffffffffu, bq.x, mask);
+                    cnd.y = __shfl_xor_sync(0xffffffffu, bq.y, mask);
+                    cnd.z = __shfl_xor_sync(0xffffffffu, bq.z, mask);
+                }
+                const float ca = iso_dist2(__fsub_rn(sa.x, cnd.x), __fsub_rn(sa.y, cnd.y), __fsub_rn(sa.z, cnd.z));
+                if (ca < best_a) {
+                    best_a = ca;
+                    bp_a = cnd;
+                }
+                const float cb = iso_dist2(__fsub_rn(sb.x, cnd.x), __fsub_rn(sb.y, cnd.y), __fsub_rn(sb.z, cnd.z));
+                if (cb < best_b) {
+                    best_b = cb;
+                    bp_b = cnd;
+                }
+            }
+        } else {
             const float alt = iso_dist2(__fsub_rn(sb.x, bp.x), __fsub_rn(sb.y, bp.y), __fsub_rn(sb.z, bp.z));
             if (alt < best_b) {
                 best_b = alt;
