@@ -316,7 +316,8 @@ __device__ __forceinline__ float2 child_dist2(const Query &q, const float4 &a, c
 // x RUN_X (x) samples.  The nearest points of one pair seed the next pair's
 // bounds (canonical distances to those real points), which keeps the
 // traversal exact and prunes almost everything but the nearest region.
-constexpr int PATCH_Z = 8, PATCH_Y = 4, WARPS_Y = QUERY_THREADS / 32, RUN_X = 8;
+constexpr int PATCH_Z = 8, PATCH_Y = 4, WARPS_Y = QUERY_THREADS / 32, RUN_X = 16;
+static_assert(RUN_X % 2 == 0, "samples go in pairs along x");
 
 __device__ __forceinline__ void load_node(const BvhNode *nodes, int cur, float4 &a, float4 &b, float4 &c, int4 &d)
 {
@@ -604,7 +605,8 @@ static int lbvh_group(iso_ctx *ctx, const SampleGrid &g, Segments sg, const int6
         // node bases are cstart[s] - s with the group-local s: shift nodes accordingly
         bb.nodes = b.nodes - base;
         const int64_t X10 = g.F / (g.Y10 * g.Z10);
-        const int64_t bricks = ((X10 + 7) / 8) * ((g.Y10 + 15) / 16) * ((g.Z10 + 7) / 8);
+        const int64_t bricks = ((X10 + RUN_X - 1) / RUN_X) * ((g.Y10 + PATCH_Y * WARPS_Y - 1) / (PATCH_Y * WARPS_Y)) *
+                               ((g.Z10 + PATCH_Z - 1) / PATCH_Z);
         bvh_query_kernel<<<dim3((unsigned)bricks, cnt), QUERY_THREADS, 0, ctx->stream>>>(
             bb, g, fields + (size_t)base * field_stride, field_stride);
         ISO_LAUNCHED(ctx);
