@@ -316,7 +316,7 @@ __device__ __forceinline__ float2 child_dist2(const Query &q, const float4 &a, c
 // x RUN_X (x) samples.  The nearest points of one pair seed the next pair's
 // bounds (canonical distances to those real points), which keeps the
 // traversal exact and prunes almost everything but the nearest region.
-constexpr int PATCH_Z = 8, PATCH_Y = 4, WARPS_Y = QUERY_THREADS / 32, RUN_X = 16;
+constexpr int PATCH_Z = 8, PATCH_Y = 4, WARPS_Y = QUERY_THREADS / 32, RUN_X = 32;
 static_assert(RUN_X % 2 == 0, "samples go in pairs along x");
 
 __device__ __forceinline__ void load_node(const BvhNode *nodes, int cur, float4 &a, float4 &b, float4 &c, int4 &d)
