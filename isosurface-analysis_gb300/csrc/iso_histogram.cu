@@ -205,7 +205,7 @@ __device__ __forceinline__ double clnc_of(const double *table, unsigned long lon
 }
 
 // Streams values [v0, v1) of one field pair (v0 a multiple of 4, rows 16-byte
-// aligned) into the shared histogram count.words (wraps to count.wrap).  Two load pairs alternate so that one is in
+// aligned) into a shared histogram through count.add4 / count.add1.  Two load pairs alternate so that one is in
 // flight while the other is binned.
 template <int MODE, class Count>
 __device__ __forceinline__ void stream_values(const Binner &bn, const float *f1, const float *f2, int64_t v0,
@@ -229,7 +229,7 @@ __device__ __forceinline__ void stream_values(const Binner &bn, const float *f1,
         }
         int c0, c1, c2, c3;
         bins4<MODE>(bn, xa, ya, c0, c1, c2, c3);
-        count4(count.words, c0, c1, c2, c3, count.wrap);
+        count.add4(c0, c1, c2, c3);
         if (qb >= n4) break;
         const int qa = qb + step;
         if (qa < n4) {
@@ -237,12 +237,12 @@ __device__ __forceinline__ void stream_values(const Binner &bn, const float *f1,
             ya = __ldg(p2 + qa);
         }
         bins4<MODE>(bn, xb, yb, c0, c1, c2, c3);
-        count4(count.words, c0, c1, c2, c3, count.wrap);
+        count.add4(c0, c1, c2, c3);
         q = qa;
     }
     for (int64_t v = v0 + ((int64_t)n4 << 2) + threadIdx.x; v < v1; v += blockDim.x) {
         const int bin = bn.mode == 2 ? 0 : exact_bucket(bn, f1[v]) * bn.bins + exact_bucket(bn, f2[v]);
-        count1(count.words, bin, count.wrap);
+        count.add1(bin);
     }
 }
 
@@ -258,10 +258,28 @@ struct EventWrap {
     }
 };
 
+// Packed 16-bit counters (two bins per word) with exact wrap handling.
 template <class Wrap>
 struct Counter {
     uint32_t *words;
     Wrap wrap;
+    __device__ __forceinline__ void add4(int b0, int b1, int b2, int b3) const { count4(words, b0, b1, b2, b3, wrap); }
+    __device__ __forceinline__ void add1(int bin) const { count1(words, bin, wrap); }
+};
+
+// One 32-bit counter per bin (histograms of up to WIDE_MAX_BINS^2 bins): no
+// halves, no wraps (a pair has fewer than 2^32 values), and the atomics'
+// results are unused.
+struct WideCounter {
+    uint32_t *words;
+    __device__ __forceinline__ void add4(int b0, int b1, int b2, int b3) const
+    {
+        atomicAdd(&words[b0], 1u);
+        atomicAdd(&words[b1], 1u);
+        atomicAdd(&words[b2], 1u);
+        atomicAdd(&words[b3], 1u);
+    }
+    __device__ __forceinline__ void add1(int bin) const { atomicAdd(&words[bin], 1u); }
 };
 
 // Interval of one pair: the union of both fields' intervals; step, reciprocal
@@ -428,6 +446,129 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
                 if (a.symmetric && i != j) {
                     a.colrow_dump[bji + c] = (uint32_t)rs;
                     a.colrow_dump[mm + bji + c] = (uint32_t)cs;
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            hxy += __shfl_xor_sync(0xffffffffu, hxy, o);
+            hx += __shfl_xor_sync(0xffffffffu, hx, o);
+            hy += __shfl_xor_sync(0xffffffffu, hy, o);
+        }
+        if (lane == 0) {
+            s_red[0][warp] = hxy;
+            s_red[1][warp] = hy;
+            s_red[2][warp] = hx;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double sxy = 0.0, sy = 0.0, sx = 0.0;
+            for (int w = 0; w < nwarps; ++w) {
+                sxy += s_red[0][w];
+                sy += s_red[1][w];
+                sx += s_red[2][w];
+            }
+            const double N = (double)a.n;
+            const double lnN = log(N);
+            sxy = sxy / N + lnN;
+            sx = sx / N + lnN;
+            sy = sy / N + lnN;
+            const double iXY = sx + sy - sxy;
+            const double val = 2.0 * iXY / (sx + sy);
+            const float out = val != val ? 0.0f : (float)val;
+            a.ism[(size_t)i * a.m + j] = out;
+            if (a.symmetric) a.ism[(size_t)j * a.m + i] = out;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 32-bit counters for up to WIDE_MAX_BINS bins
+//
+// A bins^2 histogram of 32-bit counters fits in shared memory up to 224 bins
+// (196 KB): each voxel is one plain atomic add, without the packed halves'
+// parity, increment and wrap checks.  Same tasks, bucket arithmetic and FP64
+// NMI as joint_histogram_mi_kernel.
+// ---------------------------------------------------------------------------
+
+constexpr int WIDE_MAX_BINS = 224;
+
+__global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_wide_kernel(PairArgs a)
+{
+    extern __shared__ uint32_t words[];
+    __shared__ int s_task;
+    __shared__ double s_red[3][HIST_THREADS / 32];
+    __shared__ uint32_t s_colsum[WIDE_MAX_BINS];  // marginals (n < 2^32)
+    __shared__ uint32_t s_rowsum[WIDE_MAX_BINS];
+
+    const int bins = a.bins;
+    const int nb = bins * bins;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    // with a multiple of 32 bins a warp reads part of one row; with a divisor
+    // of the block size as bins each thread reads one column
+    const bool warp_rows = (bins & 31) == 0;
+    const bool col_own = (blockDim.x % bins) == 0;
+    for (int w = threadIdx.x; w < nb; w += blockDim.x) words[w] = 0;
+
+    for (;;) {
+        if (threadIdx.x == 0) s_task = (int)atomicAdd(a.counter, 1u);
+        for (int c = threadIdx.x; c < bins; c += blockDim.x) {
+            s_colsum[c] = 0;
+            s_rowsum[c] = 0;
+        }
+        __syncthreads();
+        const int t = s_task;
+        if (t >= a.num_tasks) break;
+        const int2 task = a.tasks[t];
+        const int i = task.x, j = task.y;
+        const Binner bn = make_binner(a.mma, a.mmb, i, j, bins);
+        const float *f1 = a.fa + (size_t)i * a.stride;
+        const float *f2 = a.fb + (size_t)j * a.stride;
+        const WideCounter cnt{words};
+        if (bn.mode == 0) stream_values<0>(bn, f1, f2, 0, a.n, cnt);
+        else stream_values<1>(bn, f1, f2, 0, a.n, cnt);
+        __syncthreads();
+
+        // bins: sum(c ln c), marginals, optional dump; clears the counters
+        const bool dump = a.joint_dump != nullptr;
+        double hxy = 0.0;
+        uint32_t cs = 0;
+        for (int idx = threadIdx.x; idx < nb; idx += blockDim.x) {
+            const uint32_t c = words[idx];
+            const int r = idx / bins, col = idx - r * bins;
+            if (c) {
+                words[idx] = 0;
+                hxy -= clnc_of(a.clnc, c);
+            }
+            if (dump) {
+                a.joint_dump[(((size_t)i * a.m + j) * bins + r) * bins + col] = c;
+                if (a.symmetric && i != j) a.joint_dump[(((size_t)j * a.m + i) * bins + col) * bins + r] = c;
+            }
+            if (warp_rows) {
+                const uint32_t rs = __reduce_add_sync(0xffffffffu, c);
+                if (lane == 0 && rs) atomicAdd(&s_rowsum[r], rs);
+            } else if (c) {
+                atomicAdd(&s_rowsum[r], c);
+            }
+            if (col_own) cs += c;
+            else if (c) atomicAdd(&s_colsum[col], c);
+        }
+        if (col_own && cs) atomicAdd(&s_colsum[threadIdx.x % bins], cs);
+        __syncthreads();
+        double hx = 0.0, hy = 0.0;
+        for (int c = threadIdx.x; c < bins; c += blockDim.x) {
+            const unsigned long long cs64 = s_colsum[c], rs64 = s_rowsum[c];
+            if (cs64) hx -= clnc_of(a.clnc, cs64);
+            if (rs64) hy -= clnc_of(a.clnc, rs64);
+            if (a.colrow_dump) {
+                const size_t mm = (size_t)a.m * a.m * bins;
+                const size_t bij = ((size_t)i * a.m + j) * bins, bji = ((size_t)j * a.m + i) * bins;
+                a.colrow_dump[bij + c] = (uint32_t)cs64;
+                a.colrow_dump[mm + bij + c] = (uint32_t)rs64;
+                if (a.symmetric && i != j) {
+                    a.colrow_dump[bji + c] = (uint32_t)rs64;
+                    a.colrow_dump[mm + bji + c] = (uint32_t)cs64;
                 }
             }
         }
@@ -849,6 +990,40 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
             joint_mi_kernel<<<np, 256, 0, ctx->stream>>>(ma);
             ISO_LAUNCHED(ctx);
         }
+        return ISO_OK;
+    }
+    if (bins <= WIDE_MAX_BINS) {
+        // 32-bit counters: no wrap events
+        const size_t wsmem = (size_t)bins * bins * sizeof(uint32_t);
+        ISO_CUDA(cudaFuncSetAttribute(joint_histogram_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(WIDE_MAX_BINS * WIDE_MAX_BINS * sizeof(uint32_t))));
+        int per_sm_w = 0;
+        ISO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_w, joint_histogram_wide_kernel, HIST_THREADS,
+                                                               wsmem));
+        if (per_sm_w < 1) per_sm_w = 1;
+        const int grid_w = std::min(ctx->num_sms * per_sm_w, num_tasks);
+        PairArgs w;
+        w.fa = d_fields_a;
+        w.fb = fb;
+        w.n = n;
+        w.stride = stride;
+        w.mma = d_minmax_a;
+        w.mmb = mmb;
+        w.tasks = (const int2 *)d_tasks;
+        w.num_tasks = num_tasks;
+        w.m = m;
+        w.bins = bins;
+        w.symmetric = symmetric ? 1 : 0;
+        w.ism = d_ism;
+        w.events = nullptr;
+        w.event_cap = 0;
+        w.clnc = (const double *)d_clnc;
+        w.counter = (unsigned int *)d_counter;
+        w.error = (int *)d_counter + 1;
+        w.joint_dump = d_joint_dump;
+        w.colrow_dump = d_colrow_dump;
+        joint_histogram_wide_kernel<<<grid_w, HIST_THREADS, wsmem, ctx->stream>>>(w);
+        ISO_LAUNCHED(ctx);
         return ISO_OK;
     }
     ISO_CUDA(cudaFuncSetAttribute(joint_histogram_mi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

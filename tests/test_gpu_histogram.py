@@ -34,7 +34,8 @@ def test_golden_small_reference_named_entry():
     assert np.abs(sim - g["sim"]).max() < TOL_REF
 
 
-@pytest.mark.parametrize("m,n,bins", [(6, 300001, 256), (9, 70001, 128), (3, 4097, 32), (2, 5, 16)])
+@pytest.mark.parametrize("m,n,bins", [(6, 300001, 256), (9, 70001, 128), (3, 4097, 32), (2, 5, 16),
+                                      (4, 50001, 224), (4, 50001, 226)])
 def test_joint_histograms_bit_exact(ctx, m, n, bins):
     f = fields_like_df(m, n, seed=m * 7 + bins)
     ism, joint = ctx.similarity_map(f, bins, joint=True)
@@ -120,20 +121,28 @@ def test_bucket_boundaries_bit_exact(ctx):
             assert np.array_equal(joint[i, j], want)
 
 
-@pytest.mark.parametrize("bins", [2, 4])
+@pytest.mark.parametrize("bins", [2, 4, 256])
 def test_counter_wraps(ctx, bins):
-    """More than 65536 hits per bin in both halves of a packed counter word:
-    the wrap corrections must restore the exact counts."""
+    """More than 65536 hits per bin.  With 256 bins the kernel packs two bins
+    per 32-bit word; buckets 0 and 1 (one word) both get over 65536 hits, so
+    the wrap corrections, including the carry out of a word, must restore the
+    exact counts.  Smaller bin counts use one 32-bit counter per bin."""
     rng = np.random.default_rng(bins)
     n = 1_000_003
-    f = rng.integers(0, bins, size=(3, n)).astype(np.float32)
-    f[:, 0] = 0
-    f[:, 1] = bins - 1
+    if bins == 256:
+        f = (rng.integers(0, 2, size=(3, n)) * (1.5 / 256)).astype(np.float32)
+        f[:, 0] = 1.0  # interval [0, 1]: the two values land in buckets 0 and 1
+    else:
+        f = rng.integers(0, bins, size=(3, n)).astype(np.float32)
+        f[:, 0] = 0
+        f[:, 1] = bins - 1
     ism, joint = ctx.similarity_map(f, bins, joint=True)
     for i in range(3):
         for j in range(3):
             want, _, _ = oracle.pair_histogram(f[i], f[j], bins)
             assert np.array_equal(joint[i, j], want), (i, j)
+    if bins == 256:
+        assert joint[0, 1][:2, :2].min() > 65536
     assert np.abs(ism - oracle.similarity_map(f, bins, mode=0)).max() < TOL_F64
 
 
