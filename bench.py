@@ -219,7 +219,7 @@ def run_ours(args):
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 5), "traffic": args.hist_traffic,
                 "kernel": ("joint_histogram_seg_kernel + joint_mi_kernel" if 0 < seg_values < F
-                           else "joint_histogram_mi_kernel"),
+                           else ("joint_histogram_wide_kernel" if bins <= 224 else "joint_histogram_mi_kernel")),
                 "peak_source": peak_kind,
                 "note": "unique bytes (each field read once, one bins^2 histogram per pair); the kernel is "
                         "bound by its counter updates: see smem_atomic",

@@ -316,8 +316,10 @@ __device__ __forceinline__ float2 child_dist2(const Query &q, const float4 &a, c
 // x RUN_X (x) samples.  The nearest points of one pair seed the next pair's
 // bounds (canonical distances to those real points), which keeps the
 // traversal exact and prunes almost everything but the nearest region.
-constexpr int PATCH_Z = 8, PATCH_Y = 4, WARPS_Y = QUERY_THREADS / 32, RUN_X = 32;
-static_assert(RUN_X % 2 == 0, "samples go in pairs along x");
+constexpr int PATCH_Z = 8, PATCH_Y = 4, WARPS_Y = QUERY_THREADS / 32;
+// samples per lane along x: long runs amortise the first pair's greedy bound;
+// short runs keep enough blocks in flight for small volumes
+constexpr int RUN_X_LONG = 32, RUN_X_SHORT = 8;
 
 __device__ __forceinline__ void load_node(const BvhNode *nodes, int cur, float4 &a, float4 &b, float4 &c, int4 &d)
 {
@@ -399,8 +401,10 @@ __device__ __forceinline__ void traverse_packet2(const BvhNode *nodes, const Que
     }
 }
 
+template <int RUN_X>
 __global__ void __launch_bounds__(QUERY_THREADS) bvh_query_kernel(Bvh b, SampleGrid g, float *fields, int64_t stride)
 {
+    static_assert(RUN_X % 2 == 0, "samples go in pairs along x");
     const int s = blockIdx.y;
     const int64_t X10 = g.F / (g.Y10 * g.Z10);
     const int64_t nbz = (g.Z10 + PATCH_Z - 1) / PATCH_Z;
@@ -605,10 +609,16 @@ static int lbvh_group(iso_ctx *ctx, const SampleGrid &g, Segments sg, const int6
         // node bases are cstart[s] - s with the group-local s: shift nodes accordingly
         bb.nodes = b.nodes - base;
         const int64_t X10 = g.F / (g.Y10 * g.Z10);
-        const int64_t bricks = ((X10 + RUN_X - 1) / RUN_X) * ((g.Y10 + PATCH_Y * WARPS_Y - 1) / (PATCH_Y * WARPS_Y)) *
-                               ((g.Z10 + PATCH_Z - 1) / PATCH_Z);
-        bvh_query_kernel<<<dim3((unsigned)bricks, cnt), QUERY_THREADS, 0, ctx->stream>>>(
-            bb, g, fields + (size_t)base * field_stride, field_stride);
+        const int64_t cols = ((g.Y10 + PATCH_Y * WARPS_Y - 1) / (PATCH_Y * WARPS_Y)) * ((g.Z10 + PATCH_Z - 1) / PATCH_Z);
+        const bool long_runs = X10 >= 128;
+        const int run = long_runs ? RUN_X_LONG : RUN_X_SHORT;
+        const int64_t bricks = ((X10 + run - 1) / run) * cols;
+        if (long_runs)
+            bvh_query_kernel<RUN_X_LONG><<<dim3((unsigned)bricks, cnt), QUERY_THREADS, 0, ctx->stream>>>(
+                bb, g, fields + (size_t)base * field_stride, field_stride);
+        else
+            bvh_query_kernel<RUN_X_SHORT><<<dim3((unsigned)bricks, cnt), QUERY_THREADS, 0, ctx->stream>>>(
+                bb, g, fields + (size_t)base * field_stride, field_stride);
         ISO_LAUNCHED(ctx);
     }
     int err = 0;
