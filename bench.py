@@ -216,8 +216,16 @@ def run_ours(args):
     achieved = hist_bytes / hist_s / 1e9
     counter_peak = ctx.counter_rate(bins if bins & (bins - 1) == 0 else 256)
     updates = F * pairs / hist_s
+    # DRAM traffic of one histogram launch: --hist-traffic, else the one-pass
+    # ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the default
+    # 256^3 workload with the fused kernel
+    traffic, traffic_src = args.hist_traffic, "--hist-traffic"
+    if traffic is None and args.config == 3 and seg_values == 0 and bins == 256:
+        traffic, traffic_src = 2.80e12 + 35.7e6, "ncu capture of this workload (533.4 ms launch)"
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 5), "traffic": args.hist_traffic,
+                "frac": round(achieved / peak, 5), "traffic": traffic,
+                "traffic_source": traffic_src if traffic is not None else None,
+                "traffic_over_unique": round(traffic / hist_bytes, 1) if traffic else None,
                 "kernel": ("joint_histogram_seg_kernel + joint_mi_kernel" if 0 < seg_values < F
                            else ("joint_histogram_wide_kernel" if bins <= 224 else "joint_histogram_mi_kernel")),
                 "peak_source": peak_kind,
