@@ -243,6 +243,16 @@ __device__ __forceinline__ void store_box(BvhNode *node, int side, float3 lo, fl
     __stcg(c + 2 + side, -hi.z);
 }
 
+// Arrival count with release (this thread's box stores before it) and
+// acquire (the sibling's box stores visible after it) at device scope: one
+// ordered atomic instead of a fence on either side.
+__device__ __forceinline__ unsigned int arrive_acq_rel(unsigned int *p)
+{
+    unsigned int old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+    return old;
+}
+
 __global__ void bvh_boxes_kernel(Bvh b)
 {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -259,9 +269,7 @@ __global__ void bvh_boxes_kernel(Bvh b)
         const int parent = link >> 1, side = link & 1;
         BvhNode *node = b.nodes + nbase + parent;
         store_box(node, side, lo, hi);
-        __threadfence();
-        if (atomicAdd(&b.flags[nbase + parent], 1u) == 0) return;  // sibling not done yet
-        __threadfence();
+        if (arrive_acq_rel(&b.flags[nbase + parent]) == 0) return;  // sibling not done yet
         const float4 na = __ldcg(&node->a), nb = __ldcg(&node->b), nc = __ldcg(&node->c);
         lo = make_float3(fminf(na.x, na.y), fminf(na.z, na.w), fminf(nb.x, nb.y));
         hi = make_float3(-fminf(nb.z, nb.w), -fminf(nc.x, nc.y), -fminf(nc.z, nc.w));
