@@ -260,3 +260,20 @@ def test_nan_values_take_bucket_zero(ctx):
             b = np.where(np.isnan(f[j]), lo, f[j]).astype(np.float32)
             want, _, _ = oracle.pair_histogram(a, b, 64, iv[i], iv[j])
             assert np.array_equal(joint[i, j], want), (i, j)
+
+
+def test_reference_named_entry_256_bins():
+    """Row and column sums of the reference-named entry at 256 bins (packed
+    16-bit counters) against the oracle."""
+    import isosim
+    a = fields_like_df(3, 70001, seed=43)
+    b = fields_like_df(3, 70001, seed=44) * 1.5
+    fields = list(a) + list(b)
+    mins = [oracle.field_interval(x)[0] for x in fields]
+    maxs = [oracle.field_interval(x)[1] for x in fields]
+    sim, cols, rows = isosim.calculate_histogram_h(fields, mins, maxs, 256, multi=True)
+    for i in range(3):
+        for j in range(3):
+            joint_ij, cs, rs = oracle.pair_histogram(a[i], b[j], 256, (mins[i], maxs[i]), (mins[3 + j], maxs[3 + j]))
+            assert np.array_equal(cols[i, j], cs) and np.array_equal(rows[i, j], rs)
+            assert abs(sim[i, j] - oracle.mi_f64(joint_ij, a.shape[1])) < TOL_F64
