@@ -304,15 +304,11 @@ def cpu_baseline(vol, isos, bins, sample_scale=1.0):
     n_samp = max(1024, int(4096 * sample_scale))
 
     def df(pts):
+        # tree build + a random sample of queries, each timed inside the C code
         p = oracle.normalize_points(pts, dims)
-        t0 = time.perf_counter()
-        oracle.distance_field_kd(p, dims, 1, idx=rng.integers(0, F, 1))  # tree build + one query
-        t_build = time.perf_counter() - t0
         idx = np.random.default_rng(len(pts)).integers(0, F, n_samp)
-        t0 = time.perf_counter()
-        oracle.distance_field_kd(p, dims, 1, idx=idx)
-        t_q = (time.perf_counter() - t0 - t_build) / n_samp
-        return t_build + max(t_q, 0.0) * F
+        _, t_build, t_query = oracle.distance_field_kd_timed(p, dims, idx)
+        return t_build + t_query / n_samp * F
 
     surfaces = [p for p, _ in res if len(p)]
     with ThreadPoolExecutor(min(cores, len(surfaces))) as ex:

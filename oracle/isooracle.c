@@ -23,10 +23,12 @@
  * (fmaf where a fused multiply-add is meant), so x86-64 and aarch64 builds give
  * identical bits.
  */
+#define _POSIX_C_SOURCE 199309L /* clock_gettime */
 #include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
+#include <time.h>
 #include <string.h>
 
 #define ORC_API __attribute__((visibility("default")))
@@ -500,16 +502,27 @@ static float kd_query(const kd_tree *t, const float s[3])
 
 /* Distance field through the k-d tree; idx (may be NULL for all samples)
  * selects sample indices, out gets one value per selected sample. */
-ORC_API void orc_distance_field_kd(const float *pts, long P, int X, int Y, int Z, int ds, const long *idx, long cnt,
-                                   float *out)
+static double orc_now(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+/* As orc_distance_field_kd; build_s and query_s (may be NULL) receive the
+ * seconds spent building the tree and answering the queries. */
+ORC_API void orc_distance_field_kd_timed(const float *pts, long P, int X, int Y, int Z, int ds, const long *idx,
+                                         long cnt, float *out, double *build_s, double *query_s)
 {
     kd_tree t;
+    const double t0 = orc_now();
     t.pts = pts;
     t.idx = (int *)malloc(sizeof(int) * (size_t)P);
     t.nodes = (kd_node *)malloc(sizeof(kd_node) * (size_t)(2 * P + 1));
     t.nn = 0;
     for (long i = 0; i < P; ++i) t.idx[i] = (int)i;
     kd_build(&t, 0, (int)P);
+    const double t1 = orc_now();
     long F = (long)(X / ds) * (Y / ds) * (Z / ds);
     long total = idx ? cnt : F;
     for (long q = 0; q < total; ++q) {
@@ -518,8 +531,17 @@ ORC_API void orc_distance_field_kd(const float *pts, long P, int X, int Y, int Z
         float best = kd_query(&t, s);
         out[q] = P == 1 ? best : sqrtf(best);
     }
+    const double t2 = orc_now();
+    if (build_s) *build_s = t1 - t0;
+    if (query_s) *query_s = t2 - t1;
     free(t.idx);
     free(t.nodes);
+}
+
+ORC_API void orc_distance_field_kd(const float *pts, long P, int X, int Y, int Z, int ds, const long *idx, long cnt,
+                                   float *out)
+{
+    orc_distance_field_kd_timed(pts, P, X, Y, Z, ds, idx, cnt, out, NULL, NULL);
 }
 
 /* ------------------------------------------------------------------------- */

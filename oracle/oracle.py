@@ -50,6 +50,8 @@ def _load_oracle():
         "orc_distance_field_f32": (None, [_P, C.c_long, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
         "orc_distance_field_f64": (None, [_P, C.c_long, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
         "orc_distance_field_kd": (None, [_P, C.c_long, C.c_int, C.c_int, C.c_int, C.c_int, _P, C.c_long, _P]),
+        "orc_distance_field_kd_timed": (None, [_P, C.c_long, C.c_int, C.c_int, C.c_int, C.c_int, _P, C.c_long, _P,
+                                               _P, _P]),
         "orc_real_range": (None, [_P, C.c_long, C.c_float, C.c_float, _P, _P]),
         "orc_isovalues": (None, [_P, C.c_long, C.c_float, C.c_float, C.c_int, C.c_int, _P]),
         "orc_select_representatives": (C.c_int, [_P, C.c_int, _P, _P, C.c_int, _P]),
@@ -162,6 +164,18 @@ def distance_field_kd(pts_norm, dims, ds=1, idx=None):
         out = np.zeros(idx.size, np.float32)
         orc.orc_distance_field_kd(_p(p), p.shape[0], X, Y, Z, ds, _p(idx), idx.size, _p(out))
     return out
+
+
+def distance_field_kd_timed(pts_norm, dims, idx, ds=1):
+    """distance_field_kd on sample indices idx; returns (field values, tree
+    build seconds, query seconds), timed inside the C code."""
+    p = f32(pts_norm).reshape(-1, 3)
+    X, Y, Z = dims
+    idx = np.ascontiguousarray(idx, np.int64)
+    out = np.zeros(idx.size, np.float32)
+    tb, tq = np.zeros(1), np.zeros(1)
+    orc.orc_distance_field_kd_timed(_p(p), p.shape[0], X, Y, Z, ds, _p(idx), idx.size, _p(out), _p(tb), _p(tq))
+    return out, float(tb[0]), float(tq[0])
 
 
 def distance_field_f64(pts_norm, dims, ds=1):
