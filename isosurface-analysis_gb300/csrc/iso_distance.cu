@@ -328,6 +328,7 @@ constexpr int PATCH_Z = 8, PATCH_Y = 4, WARPS_Y = QUERY_THREADS / 32;
 // samples per lane along x: long runs amortise the first pair's greedy bound;
 // short runs keep enough blocks in flight for small volumes
 constexpr int RUN_X_LONG = 32, RUN_X_SHORT = 8;
+constexpr int QUERY_GROUP = 4;  // samples per lane traversed together
 
 __device__ __forceinline__ void load_node(const BvhNode *nodes, int cur, float4 &a, float4 &b, float4 &c, int4 &d)
 {
@@ -337,64 +338,63 @@ __device__ __forceinline__ void load_node(const BvhNode *nodes, int cur, float4 
     d = __ldg(&nodes[cur].d);
 }
 
-// Exact nearest canonical squared distances for the 64 samples of a warp (two
-// per lane, A and B), traversed as one packet: every lane evaluates every
-// visited node against both its samples and bounds, and a subtree is skipped
-// only when no sample's bound admits it (bounds only decrease, so skipping is
-// safe for every sample).  Node addresses are warp-uniform (one broadcast
-// load per node) and no lane idles.  Each best starts as the canonical
-// distance to a real point bp; on return it is the minimum and bp its point.
-__device__ __forceinline__ void traverse_packet2(const BvhNode *nodes, const Query &qa, const Query &qb, float &best_a,
-                                                 float3 &bp_a, float &best_b, float3 &bp_b, int *error)
+// Exact nearest canonical squared distances for the 32*K samples of a warp (K
+// per lane), traversed as one packet: every lane evaluates every visited node
+// against all its samples and bounds, and a subtree is skipped only when no
+// sample's bound admits it (bounds only decrease, so skipping is safe for
+// every sample).  Node addresses are warp-uniform (one broadcast load per
+// node) and no lane idles.  Each best starts as the canonical distance to a
+// real point bp; on return it is the minimum and bp its point.
+template <int K>
+__device__ __forceinline__ void traverse_packet(const BvhNode *nodes, const Query (&q)[K], float (&best)[K],
+                                                float3 (&bp)[K], int *error)
 {
-    int stack[STACK_DEPTH];     // warp-uniform node ids
-    float sda[STACK_DEPTH];     // sample A's distance to each postponed node
-    float sdb[STACK_DEPTH];     // sample B's
+    int stack[STACK_DEPTH];      // warp-uniform node ids
+    float sd[K][STACK_DEPTH];    // each sample's distance to each postponed node
     int top = 0;
     int cur = 0;
     for (;;) {
         float4 a, b, c;
         int4 d;
         load_node(nodes, cur, a, b, c, d);
-        const float2 da = child_dist2(qa, a, b, c);
-        const float2 db = child_dist2(qb, a, b, c);
+        float2 dd[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) dd[k] = child_dist2(q[k], a, b, c);
         const int left = d.x, right = d.y;
         bool gl = false, gr = false;
         if (left & LEAF_BIT) {
-            if (da.x < best_a) {
-                best_a = da.x;
-                bp_a = make_float3(a.x, a.z, b.x);
-            }
-            if (db.x < best_b) {
-                best_b = db.x;
-                bp_b = make_float3(a.x, a.z, b.x);
-            }
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                if (dd[k].x < best[k]) {
+                    best[k] = dd[k].x;
+                    bp[k] = make_float3(a.x, a.z, b.x);
+                }
         } else {
-            gl = (da.x < best_a) | (db.x < best_b);
+#pragma unroll
+            for (int k = 0; k < K; ++k) gl |= dd[k].x < best[k];
         }
         if (right & LEAF_BIT) {
-            if (da.y < best_a) {
-                best_a = da.y;
-                bp_a = make_float3(a.y, a.w, b.y);
-            }
-            if (db.y < best_b) {
-                best_b = db.y;
-                bp_b = make_float3(a.y, a.w, b.y);
-            }
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                if (dd[k].y < best[k]) {
+                    best[k] = dd[k].y;
+                    bp[k] = make_float3(a.y, a.w, b.y);
+                }
         } else {
-            gr = (da.y < best_a) | (db.y < best_b);
+#pragma unroll
+            for (int k = 0; k < K; ++k) gr |= dd[k].y < best[k];
         }
         const bool any_l = __any_sync(0xffffffffu, gl), any_r = __any_sync(0xffffffffu, gr);
         if (any_l && any_r) {
-            // most lanes' nearer child (for sample A) first
-            const bool lfirst = __popc(__ballot_sync(0xffffffffu, da.x <= da.y)) >= 16;
+            // most lanes' nearer child (for the first sample) first
+            const bool lfirst = __popc(__ballot_sync(0xffffffffu, dd[0].x <= dd[0].y)) >= 16;
             if (top == STACK_DEPTH) {
                 atomicExch(error, 2);
                 break;
             }
             stack[top] = lfirst ? right : left;
-            sda[top] = lfirst ? da.y : da.x;
-            sdb[top] = lfirst ? db.y : db.x;
+#pragma unroll
+            for (int k = 0; k < K; ++k) sd[k][top] = lfirst ? dd[k].y : dd[k].x;
             ++top;
             cur = lfirst ? left : right;
         } else if (any_l) {
@@ -402,17 +402,24 @@ __device__ __forceinline__ void traverse_packet2(const BvhNode *nodes, const Que
         } else if (any_r) {
             cur = right;
         } else {
-            while (top > 0 && !__any_sync(0xffffffffu, (sda[top - 1] < best_a) | (sdb[top - 1] < best_b))) --top;
+            for (;;) {
+                if (top == 0) break;
+                bool keep = false;
+#pragma unroll
+                for (int k = 0; k < K; ++k) keep |= sd[k][top - 1] < best[k];
+                if (__any_sync(0xffffffffu, keep)) break;
+                --top;
+            }
             if (top == 0) break;
             cur = stack[--top];
         }
     }
 }
 
-template <int RUN_X>
+template <int RUN_X, int K>
 __global__ void __launch_bounds__(QUERY_THREADS) bvh_query_kernel(Bvh b, SampleGrid g, float *fields, int64_t stride)
 {
-    static_assert(RUN_X % 2 == 0, "samples go in pairs along x");
+    static_assert(RUN_X % K == 0 && K >= 2, "samples go in groups of K along x");
     const int s = blockIdx.y;
     const int64_t X10 = g.F / (g.Y10 * g.Z10);
     const int64_t nbz = (g.Z10 + PATCH_Z - 1) / PATCH_Z;
@@ -476,62 +483,62 @@ __global__ void __launch_bounds__(QUERY_THREADS) bvh_query_kernel(Bvh b, SampleG
     }
     // every lane runs every step (the packet traversal needs the whole warp);
     // lanes past the grid edge repeat a valid sample and do not store
-    float3 bq = bp;  // nearest point of the previous pair's second sample
+    // nearest points of the previous group's last two samples
+    float3 p_last = bp, p_prev = bp;
     // y and z coordinates are fixed per lane (the sample-grid formula of
     // BVH.cu:393-406, as sample_point computes it)
     const float sy = __fdiv_rn((float)(yc * g.ds + g.ds / 2), (float)g.Y);
     const float sz = __fdiv_rn((float)(zc * g.ds + g.ds / 2), (float)g.Z);
-    for (int k = 0; k < RUN_X; k += 2) {
-        const int64_t xa = x0 + k, xb = x0 + k + 1;
-        if (!__any_sync(0xffffffffu, col_valid && xa < X10)) break;
-        const bool va = col_valid && xa < X10, vb = col_valid && xb < X10;
-        const int64_t xac = xa < X10 ? xa : X10 - 1, xbc = xb < X10 ? xb : X10 - 1;
-        const int64_t ia = (xac * g.Y10 + yc) * g.Z10 + zc;
-        const int64_t ib = (xbc * g.Y10 + yc) * g.Z10 + zc;
-        const float3 sa = make_float3(__fdiv_rn((float)(xac * g.ds + g.ds / 2), (float)g.X), sy, sz);
-        const float3 sb = make_float3(__fdiv_rn((float)(xbc * g.ds + g.ds / 2), (float)g.X), sy, sz);
-        // bounds: the nearest of the previous pair's nearest points, this
-        // lane's and its z and y neighbours' (for the first pair, the greedy
-        // candidate of sample A)
-        float best_a = k == 0 ? best : iso_dist2(__fsub_rn(sa.x, bq.x), __fsub_rn(sa.y, bq.y), __fsub_rn(sa.z, bq.z));
-        float3 bp_a = k == 0 ? bp : bq;
-        float best_b = iso_dist2(__fsub_rn(sb.x, bq.x), __fsub_rn(sb.y, bq.y), __fsub_rn(sb.z, bq.z));
-        float3 bp_b = bq;
-        if (k > 0) {
+    for (int k0 = 0; k0 < RUN_X; k0 += K) {
+        if (!__any_sync(0xffffffffu, col_valid && x0 + k0 < X10)) break;
+        // candidates (all real points, so every bound is a true distance):
+        // the previous group's last two nearest points and the z and y
+        // neighbour lanes' last one (for the first group, the greedy points)
+        float3 cand[4];
+        cand[0] = p_last;
+        cand[1] = p_prev;
 #pragma unroll
-            for (int o = 0; o < 3; ++o) {
-                const int mask = o == 0 ? 0 : (o == 1 ? 1 : PATCH_Z);
-                float3 cnd;
-                if (o == 0) {
-                    cnd = bp;
-                } else {
-                    cnd.x = __shfl_xor_sync(0xffffffffu, bq.x, mask);
-                    cnd.y = __shfl_xor_sync(0xffffffffu, bq.y, mask);
-                    cnd.z = __shfl_xor_sync(0xffffffffu, bq.z, mask);
-                }
-                const float ca = iso_dist2(__fsub_rn(sa.x, cnd.x), __fsub_rn(sa.y, cnd.y), __fsub_rn(sa.z, cnd.z));
-                if (ca < best_a) {
-                    best_a = ca;
-                    bp_a = cnd;
-                }
-                const float cb = iso_dist2(__fsub_rn(sb.x, cnd.x), __fsub_rn(sb.y, cnd.y), __fsub_rn(sb.z, cnd.z));
-                if (cb < best_b) {
-                    best_b = cb;
-                    bp_b = cnd;
-                }
+        for (int o = 0; o < 2; ++o) {
+            const int mask = o == 0 ? 1 : PATCH_Z;
+            cand[2 + o].x = __shfl_xor_sync(0xffffffffu, p_last.x, mask);
+            cand[2 + o].y = __shfl_xor_sync(0xffffffffu, p_last.y, mask);
+            cand[2 + o].z = __shfl_xor_sync(0xffffffffu, p_last.z, mask);
+        }
+        Query q[K];
+        float bst[K];
+        float3 pts[K];
+        int64_t idx[K];
+        bool val[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int64_t x = x0 + k0 + k;
+            val[k] = col_valid && x < X10;
+            const int64_t xc = x < X10 ? x : X10 - 1;
+            idx[k] = (xc * g.Y10 + yc) * g.Z10 + zc;
+            const float3 sk = make_float3(__fdiv_rn((float)(xc * g.ds + g.ds / 2), (float)g.X), sy, sz);
+            q[k] = make_query(sk);
+            bst[k] = iso_dist2(__fsub_rn(sk.x, cand[0].x), __fsub_rn(sk.y, cand[0].y), __fsub_rn(sk.z, cand[0].z));
+            pts[k] = cand[0];
+            if (k0 == 0 && k == 0) {
+                bst[k] = best;  // the greedy bound of this very sample
+                pts[k] = bp;
             }
-        } else {
-            const float alt = iso_dist2(__fsub_rn(sb.x, bp.x), __fsub_rn(sb.y, bp.y), __fsub_rn(sb.z, bp.z));
-            if (alt < best_b) {
-                best_b = alt;
-                bp_b = bp;
+#pragma unroll
+            for (int o = 1; o < 4; ++o) {
+                const float cd = iso_dist2(__fsub_rn(sk.x, cand[o].x), __fsub_rn(sk.y, cand[o].y),
+                                           __fsub_rn(sk.z, cand[o].z));
+                if (cd < bst[k]) {
+                    bst[k] = cd;
+                    pts[k] = cand[o];
+                }
             }
         }
-        traverse_packet2(nodes, make_query(sa), make_query(sb), best_a, bp_a, best_b, bp_b, b.error);
-        if (va) out[ia] = __fsqrt_rn(best_a);
-        if (vb) out[ib] = __fsqrt_rn(best_b);
-        bp = bp_a;
-        bq = bp_b;
+        traverse_packet<K>(nodes, q, bst, pts, b.error);
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (val[k]) out[idx[k]] = __fsqrt_rn(bst[k]);
+        p_last = pts[K - 1];
+        p_prev = pts[K - 2];
     }
 }
 
@@ -622,10 +629,10 @@ static int lbvh_group(iso_ctx *ctx, const SampleGrid &g, Segments sg, const int6
         const int run = long_runs ? RUN_X_LONG : RUN_X_SHORT;
         const int64_t bricks = ((X10 + run - 1) / run) * cols;
         if (long_runs)
-            bvh_query_kernel<RUN_X_LONG><<<dim3((unsigned)bricks, cnt), QUERY_THREADS, 0, ctx->stream>>>(
+            bvh_query_kernel<RUN_X_LONG, QUERY_GROUP><<<dim3((unsigned)bricks, cnt), QUERY_THREADS, 0, ctx->stream>>>(
                 bb, g, fields + (size_t)base * field_stride, field_stride);
         else
-            bvh_query_kernel<RUN_X_SHORT><<<dim3((unsigned)bricks, cnt), QUERY_THREADS, 0, ctx->stream>>>(
+            bvh_query_kernel<RUN_X_SHORT, QUERY_GROUP><<<dim3((unsigned)bricks, cnt), QUERY_THREADS, 0, ctx->stream>>>(
                 bb, g, fields + (size_t)base * field_stride, field_stride);
         ISO_LAUNCHED(ctx);
     }
