@@ -493,10 +493,16 @@ def run_multi(args):
     ctx = isosim.Context(local)
     stats = {"ism_pairs": 0, "t_ism": 0.0}
 
+    # this rank's volumes are generated before the timed batch (the engine's
+    # input, like a volume loaded from disk)
+    vlo, vhi = multi.shard(V * T, rank, world)
+    volumes = {vid: volume(vid // T, vid % T) for vid in range(vlo, vhi)}
+    torch.cuda.synchronize()
+
     def local_fields(lo, hi):
         rows = torch.zeros(((hi - lo) * reps, stride), dtype=torch.float32, device="cuda")
         for vid in range(lo, hi):
-            vol = volume(vid // T, vid % T)
+            vol = volumes[vid]
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             vmin, vmax = float(vol.min()), float(vol.max())
