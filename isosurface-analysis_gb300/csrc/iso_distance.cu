@@ -417,7 +417,7 @@ __device__ __forceinline__ void traverse_packet(const BvhNode *nodes, const Quer
 }
 
 template <int RUN_X, int K>
-__global__ void __launch_bounds__(QUERY_THREADS) bvh_query_kernel(Bvh b, SampleGrid g, float *fields, int64_t stride)
+__global__ void __launch_bounds__(QUERY_THREADS, 8) bvh_query_kernel(Bvh b, SampleGrid g, float *fields, int64_t stride)
 {
     static_assert(RUN_X % K == 0 && K >= 2, "samples go in groups of K along x");
     const int s = blockIdx.y;
