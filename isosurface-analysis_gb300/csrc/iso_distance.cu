@@ -13,10 +13,11 @@
 //    memory in tiles (plain FP32 comparator path);
 //  * LBVH: all point sets at once -- 30-bit Morton codes (BVH.cu:84-117), one
 //    radix sort of (set, code) keys, Karras hierarchy per set with ties broken
-//    by index (exact for duplicate codes), bottom-up boxes with release/acquire
-//    fences, then a stack traversal per sample.  A child box is skipped only if
-//    its canonical box distance is >= the best squared distance so far; the box
-//    distance is the same fma chain over per-axis gaps, which never exceeds the
+//    by index (exact for duplicate codes), bottom-up boxes (acquire-release
+//    arrival counts), then warp packet traversals (four samples per lane).  A
+//    child box is skipped only if its canonical box distance is >= the best
+//    squared distance so far; the box distance is the same fma chain over
+//    per-axis gaps, which never exceeds the
 //    canonical distance of any point inside (rounding is monotone), so the
 //    minimum equals the brute-force minimum bit for bit.
 #include <cub/cub.cuh>

@@ -35,7 +35,7 @@ def test_golden_small_reference_named_entry():
 
 
 @pytest.mark.parametrize("m,n,bins", [(6, 300001, 256), (9, 70001, 128), (3, 4097, 32), (2, 5, 16),
-                                      (4, 50001, 224), (4, 50001, 226)])
+                                      (4, 50001, 224), (4, 50001, 226), (3, 20001, 100), (3, 9999, 62)])
 def test_joint_histograms_bit_exact(ctx, m, n, bins):
     f = fields_like_df(m, n, seed=m * 7 + bins)
     ism, joint = ctx.similarity_map(f, bins, joint=True)
