@@ -210,24 +210,30 @@ def run_ours(args):
     # bytes = each distance field read once + each joint histogram written once
     F = X * Y * Z
     hist_bytes = 4.0 * F * m + 4.0 * bins * bins * pairs
-    seg_values = 0 if args.hist_seg is None else args.hist_seg
+    seg_values = 2097152 if args.hist_seg is None else args.hist_seg  # the engine's default
     hist_s = stage[2] / 1e3
     peak, peak_kind = load_peaks()
     achieved = hist_bytes / hist_s / 1e9
     counter_peak = ctx.counter_rate(bins if bins & (bins - 1) == 0 else 256)
     updates = F * pairs / hist_s
-    # DRAM traffic of one histogram launch: --hist-traffic, else the one-pass
-    # ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the default
-    # 256^3 workload with the fused kernel
+    # DRAM traffic of the histogram stage: --hist-traffic, else one-pass ncu
+    # captures (dram__bytes_read.sum + dram__bytes_write.sum) of the default
+    # 256^3 workload: the segment-major schedule (8 chunks: 8 segment-kernel
+    # and 8 NMI-kernel launches, summed) or the one-CTA-per-pair kernel
     traffic, traffic_src = args.hist_traffic, "--hist-traffic"
-    if traffic is None and args.config == 3 and seg_values == 0 and bins == 256:
-        traffic, traffic_src = 2.80e12 + 35.7e6, "ncu capture of this workload (533.4 ms launch)"
+    if traffic is None and args.config == 3 and bins == 256:
+        if seg_values == 2097152:
+            traffic = 1.4799e12 + 12.25e9 + 8.613e9 + 2.6e6
+            traffic_src = "ncu capture of this workload (16 launches of the stage, 517 ms)"
+        elif seg_values == 0:
+            traffic, traffic_src = 2.80e12 + 35.7e6, "ncu capture of this workload (one launch, 533.4 ms)"
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 5), "traffic": traffic,
                 "traffic_source": traffic_src if traffic is not None else None,
                 "traffic_over_unique": round(traffic / hist_bytes, 1) if traffic else None,
-                "kernel": ("joint_histogram_seg_kernel + joint_mi_kernel" if 0 < seg_values < F
-                           else ("joint_histogram_wide_kernel" if bins <= 224 else "joint_histogram_mi_kernel")),
+                "kernel": ("joint_histogram_wide_kernel" if bins <= 224 else
+                           ("joint_histogram_seg_kernel + joint_mi_kernel" if 0 < seg_values < F
+                            else "joint_histogram_mi_kernel")),
                 "peak_source": peak_kind,
                 "note": "unique bytes (each field read once, one bins^2 histogram per pair); the kernel is "
                         "bound by its counter updates: see smem_atomic",

@@ -109,10 +109,11 @@ ISO_API int64_t iso_ctx_launches(iso_ctx *ctx);
 /* Tunable limits of a context. */
 #define ISO_LIMIT_LBVH_GROUP_POINTS 1 /* LBVHs are built for groups of surfaces of at most this many
                                           points (default 2^27), bounding their device memory */
-#define ISO_LIMIT_HIST_SEGMENT_VALUES 2 /* fields longer than this are histogrammed segment by segment
-                                            (all running pairs on the same slice of their fields);
-                                            0 = never (the default); otherwise a multiple of 4,
-                                            at least 65536 */
+#define ISO_LIMIT_HIST_SEGMENT_VALUES 2 /* histograms of 226..256 bins over fields longer than this
+                                            run segment by segment (all running pairs on the same
+                                            slice of their fields; up to 1 GB of per-pair histograms);
+                                            0 = never; otherwise a multiple of 4, at least 65536;
+                                            default 2097152 */
 ISO_API int iso_ctx_set_limit(iso_ctx *ctx, int which, int64_t value);
 
 /* ---------------------------------------------------------------------- */

@@ -492,7 +492,7 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
 // NMI as joint_histogram_mi_kernel.
 // ---------------------------------------------------------------------------
 
-constexpr int WIDE_MAX_BINS = 224;
+constexpr int WIDE_MAX_BINS = ISO_WIDE_MAX_BINS;
 
 __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_wide_kernel(PairArgs a)
 {
@@ -935,16 +935,17 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
 
     const size_t smem = (size_t)bins * bins / 2 * sizeof(uint32_t);
     const int64_t seg_len = ctx->hist_segment_values;
-    if (seg_len > 0 && n > seg_len) {
-        // long fields: segment-major schedule, pairs in chunks bounding the
-        // global histograms to about 2 GB (and the task count to int range)
+    if (seg_len > 0 && n > seg_len && bins > WIDE_MAX_BINS) {
+        // long fields, packed counters: segment-major schedule, pairs in chunks
+        // bounding the global histograms to ISO_HIST_CHUNK_BYTES (and the task
+        // count to int range)
         ISO_CUDA(cudaFuncSetAttribute(joint_histogram_seg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)(ISO_MAX_BINS * ISO_MAX_BINS / 2 * sizeof(uint32_t))));
         const size_t hist_bytes = (size_t)bins * bins * sizeof(uint32_t);
         const int64_t num_segs64 = (n + seg_len - 1) / seg_len;
         if (num_segs64 > (1 << 24)) return iso_fail(ISO_ERR_ARG, "histogram segments: %lld too many", (long long)num_segs64);
         const int num_segs = (int)num_segs64;
-        size_t chunk_sz = std::min<size_t>((size_t)num_tasks, ((size_t)2 << 30) / hist_bytes);
+        size_t chunk_sz = std::min<size_t>((size_t)num_tasks, ISO_HIST_CHUNK_BYTES / hist_bytes);
         chunk_sz = std::min<size_t>(chunk_sz, (size_t)(((int64_t)1 << 30) / num_segs64));
         const int chunk = (int)std::max<size_t>(1, chunk_sz);
         const int group = (int)std::max<size_t>(1, std::min<size_t>(1024, ((size_t)32 << 20) / hist_bytes));

@@ -44,7 +44,9 @@ void iso_clear_error();
 constexpr int ISO_MAX_BINS = 256;
 // LBVH surfaces are built and queried in groups of at most this many points
 // (default of iso_ctx_set_limit(ISO_LIMIT_LBVH_GROUP_POINTS))
-constexpr int64_t ISO_HIST_SEGMENT_VALUES = 0;  // fused kernel by default (faster at 256^3)
+constexpr int64_t ISO_HIST_SEGMENT_VALUES = 2097152;  // segment-major above 2^21 values (226..256 bins)
+constexpr int ISO_WIDE_MAX_BINS = 224;                // up to this many bins: 32-bit counters, one CTA per pair
+constexpr size_t ISO_HIST_CHUNK_BYTES = (size_t)1 << 30;  // per-pair global histograms of one segment-major chunk
 constexpr int64_t ISO_LBVH_GROUP_POINTS = (int64_t)1 << 27;
 
 // ---------------------------------------------------------------------------
@@ -102,7 +104,7 @@ struct iso_ctx {
     // admission hook: called by iso_ism once the surface counts fix the
     // request's device-memory need; a non-zero return aborts the request
     int64_t lbvh_group_points = ISO_LBVH_GROUP_POINTS;  // see iso_ctx_set_limit
-    int64_t hist_segment_values = ISO_HIST_SEGMENT_VALUES;  // 0: fused kernel for every length
+    int64_t hist_segment_values = ISO_HIST_SEGMENT_VALUES;  // 0: one CTA per pair for every length
     int (*admit)(void *user, size_t bytes) = nullptr;
     void *admit_user = nullptr;
     // request shape for the admission estimate (set by iso_ism)

@@ -542,6 +542,12 @@ int iso_run_surfaces(iso_ctx *ctx, const float *d_vol, int X, int Y, int Z, cons
                       (ctx->plan_lbvh ? 180.0 * std::min(P, (double)ctx->lbvh_group_points) : 0.0) +
                       4.0 * m * ctx->plan_stride + 12.0 * m * m +
                       8.0 * 65536 + 16.0 * (1 << 20);
+        // segment-major histograms keep one chunk of per-pair global histograms
+        if (ctx->hist_segment_values > 0 && ctx->plan_stride > ctx->hist_segment_values &&
+            ctx->plan_bins > ISO_WIDE_MAX_BINS) {
+            const double hist = 4.0 * ctx->plan_bins * ctx->plan_bins;
+            need += std::min(m * (m + 1) / 2 * hist, (double)ISO_HIST_CHUNK_BYTES);
+        }
         need *= 1.15;  // arena growth slack
         if (ctx->admit(ctx->admit_user, (size_t)need) != 0)
             return iso_fail(ISO_ERR_NOMEM, "request needs %.0f bytes of device memory; over the budget", need);

@@ -149,6 +149,7 @@ def test_counter_wraps(ctx, bins):
 # ---- segment-major schedule (fields longer than one 262144-value segment) ----
 
 SEG = 262144
+DEFAULT_SEG = 2097152  # the engine's default segment length
 
 
 @pytest.fixture
@@ -157,7 +158,7 @@ def seg_mode(ctx):
     than SEG values (off by default)."""
     ctx.set_hist_segment_values(SEG)
     yield
-    ctx.set_hist_segment_values(0)
+    ctx.set_hist_segment_values(DEFAULT_SEG)
 
 
 @pytest.mark.usefixtures("seg_mode")
@@ -178,17 +179,18 @@ def test_segmented_bit_exact(ctx, n):
 
 @pytest.mark.usefixtures("seg_mode")
 def test_segmented_wraps_in_both_halves(ctx):
-    """Constant fields put every value of a segment in one bin (four 16-bit
-    wraps per segment): the even bin (low half, carries into the high half),
-    the odd bin (high half, carry out of the word) and a word whose halves
-    both wrap."""
+    """Fields of two values that land in buckets 0 and 1 of 256 (one packed
+    word): whole segments go to one bin (four 16-bit wraps per segment), to
+    the even bin (low half, carries into the high half), the odd bin (high
+    half, carry out of the word) and both halves of one word."""
     n = 4 * SEG + 3
-    bins = 2
+    bins = 256
     rng = np.random.default_rng(5)
-    half = (rng.uniform(0, 1, n) < 0.5).astype(np.float32)
-    f = np.stack([np.zeros(n, np.float32), np.ones(n, np.float32), half, 1 - half])
-    f[0, 0] = 1.0   # give the constant fields a non-empty range
-    f[1, 0] = 0.0
+    lo_v, hi_v = np.float32(0.0), np.float32(1.5 / 256)
+    half = np.where(rng.uniform(0, 1, n) < 0.5, lo_v, hi_v).astype(np.float32)
+    f = np.stack([np.full(n, lo_v, np.float32), np.full(n, hi_v, np.float32), half,
+                  np.where(half == lo_v, hi_v, lo_v).astype(np.float32)])
+    f[:, 0] = 1.0   # every field spans [0, 1]: the two values are buckets 0 and 1
     ism, joint = ctx.similarity_map(f, bins, joint=True)
     for i in range(4):
         for j in range(4):
@@ -199,19 +201,22 @@ def test_segmented_wraps_in_both_halves(ctx):
 
 @pytest.mark.usefixtures("seg_mode")
 def test_segmented_cross_map_and_sums(ctx):
+    """Cross map on the session context (262,144-value segments) and the
+    reference-named entry on the default one (fields just over the default
+    segment length, so it runs segment-major too, with row and column sums)."""
     import isosim
-    n = 2 * SEG + 5
+    n = DEFAULT_SEG + 5
     a = fields_like_df(3, n, seed=31)
     b = fields_like_df(3, n, seed=32) * 1.5
-    cm = ctx.cross_map(a, b, 128)
+    cm = ctx.cross_map(a, b, 256)
     fields = list(a) + list(b)
     mins = [oracle.field_interval(x)[0] for x in fields]
     maxs = [oracle.field_interval(x)[1] for x in fields]
-    sim, cols, rows = isosim.calculate_histogram_h(fields, mins, maxs, 128, multi=True)
+    sim, cols, rows = isosim.calculate_histogram_h(fields, mins, maxs, 256, multi=True)
     assert np.abs(sim - cm).max() < TOL_F64
     for i in range(3):
         for j in range(3):
-            joint, cs, rs = oracle.pair_histogram(a[i], b[j], 128, (mins[i], maxs[i]), (mins[3 + j], maxs[3 + j]))
+            joint, cs, rs = oracle.pair_histogram(a[i], b[j], 256, (mins[i], maxs[i]), (mins[3 + j], maxs[3 + j]))
             assert abs(cm[i, j] - oracle.mi_f64(joint, n)) < TOL_F64
             assert np.array_equal(cols[i, j], cs) and np.array_equal(rows[i, j], rs)
 
@@ -239,7 +244,7 @@ def test_schedules_agree(ctx):
         ctx.set_hist_segment_values(SEG)
         ism2, j2 = ctx.similarity_map(f, 256, joint=True)
     finally:
-        ctx.set_hist_segment_values(0)
+        ctx.set_hist_segment_values(DEFAULT_SEG)
     assert np.array_equal(j0, j1) and np.array_equal(j0, j2)
     assert np.abs(ism0 - ism1).max() < TOL_F64 and np.abs(ism0 - ism2).max() < TOL_F64
 
