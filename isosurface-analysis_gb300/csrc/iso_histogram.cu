@@ -73,25 +73,22 @@ __device__ __noinline__ int4 exact_bins4(float mn, float step, int bins, float4 
 }
 
 // ---- fixed-point bucket ----------------------------------------------------
-// s = RN(RN(v - mn) * r + 1536), r = RN(1/step), in one packed FMA for two
-// values.  1536 = 1.5 * 2^10, so s lies in [1536, 2048) where the float ulp
-// is 2^-13: the low bits of s are q' = s - 1536 as a fixed-point number with
-// 13 fraction bits, u = bits(s) - bits(1536) = q' * 2^13.
-//
-// q' differs from the reference's quotient q = RN(RN(v - mn) / step) by less
-// than 2^-13: 2^-14 (rounding of s) + q * 2^-24 (r) + 2^-17 (rounding of q,
-// q < 256) <= 1.375 * 2^-14.  So floor(q') = floor(q) unless q' is an integer
-// (u a multiple of 2^13), where q may lie just below it; those values take
-// the division.  u = 0 (v == mn, q = 0) is exact.  Near q = bins both sides
-// clamp to the last bucket, so that boundary needs no check.
+// With d = RN(v - mn) and r = RN(1/step), two packed FMAs per two values:
+//   t = RD(d * r + 2^23) = 2^23 + floor(d * r) (ulp 1 in [2^23, 2^24)), so the
+//     bucket candidate floor(d * r) is the low mantissa bits of t;
+//   s = RN(d * r + 1536): 1536 = 1.5 * 2^10, so s lies in [1536, 2048) where
+//     the float ulp is 2^-13: u = bits(s) - bits(1536) is d * r rounded to a
+//     fixed-point number with 13 fraction bits.
+// d * r differs from the reference's quotient q = RN(d / step) by less than
+// q * 2^-24 (r) + 2^-17 (rounding of q, q < 256) < 2^-15, so floor(d * r) =
+// floor(q) unless d * r lies within 2^-15 of a nonzero integer, and then s
+// (within 2^-14 of d * r) is that integer: values whose s is a nonzero
+// integer (u a nonzero multiple of 2^13) take the division.  u = 0 means
+// d * r < 2^-14, where both floors are 0.  Near q = bins both sides clamp to
+// the last bucket, so that boundary needs no check.
 constexpr float FX_BASE = 1536.0f;
-constexpr uint32_t FX_BASE_BITS = 0x44C00000u;
-constexpr int FX_FRAC = 13;
-
-__device__ __forceinline__ float2 fx_pair(float a, float b, float2 neg_mn, float2 r)
-{
-    return __ffma2_rn(__fadd2_rn(make_float2(a, b), neg_mn), r, make_float2(FX_BASE, FX_BASE));
-}
+constexpr float FLOOR_BASE = 8388608.0f;  // 2^23
+constexpr uint32_t FLOOR_BASE_BITS = 0x4B000000u;
 
 // Bins (row = field-1 bucket, column = field-2 bucket) of the four voxels in x, y.
 template <int MODE>
@@ -101,20 +98,35 @@ __device__ __forceinline__ void bins4(const Binner &bn, const float4 &x, const f
     const int bins = bn.bins;
     if (MODE == 0) {
         const float2 nm = make_float2(-bn.mn, -bn.mn), rr = make_float2(bn.r, bn.r);
-        const float2 sx01 = fx_pair(x.x, x.y, nm, rr), sx23 = fx_pair(x.z, x.w, nm, rr);
-        const float2 sy01 = fx_pair(y.x, y.y, nm, rr), sy23 = fx_pair(y.z, y.w, nm, rr);
+        const float2 dx01 = __fadd2_rn(make_float2(x.x, x.y), nm), dx23 = __fadd2_rn(make_float2(x.z, x.w), nm);
+        const float2 dy01 = __fadd2_rn(make_float2(y.x, y.y), nm), dy23 = __fadd2_rn(make_float2(y.z, y.w), nm);
+        // s: the quotient on the 2^-13 grid (for the ambiguity test below)
+        const float2 cs = make_float2(FX_BASE, FX_BASE);
+        const float2 sx01 = __ffma2_rn(dx01, rr, cs), sx23 = __ffma2_rn(dx23, rr, cs);
+        const float2 sy01 = __ffma2_rn(dy01, rr, cs), sy23 = __ffma2_rn(dy23, rr, cs);
         const uint32_t ux0 = __float_as_uint(sx01.x), ux1 = __float_as_uint(sx01.y);
         const uint32_t ux2 = __float_as_uint(sx23.x), ux3 = __float_as_uint(sx23.y);
         const uint32_t uy0 = __float_as_uint(sy01.x), uy1 = __float_as_uint(sy01.y);
         const uint32_t uy2 = __float_as_uint(sy23.x), uy3 = __float_as_uint(sy23.y);
-        // bucket = min((u >> 13) - (bits(1536) >> 13), bins - 1) as unsigned:
-        // any input (also one outside the interval) stays inside the histogram
-        const uint32_t kb = FX_BASE_BITS >> FX_FRAC;
+        // t = RD(d * r + 2^23) = 2^23 + floor(d * r): the bucket is its low
+        // mantissa bits, with no shift.  floor(d * r) equals the reference's
+        // bucket except where s is ambiguous (within 2^-14 of an integer
+        // covers the 2^-15 between d * r and the reference's quotient).
+        const float2 ct = make_float2(FLOOR_BASE, FLOOR_BASE);
+        const float2 tx01 = __ffma2_rd(dx01, rr, ct), tx23 = __ffma2_rd(dx23, rr, ct);
+        const float2 ty01 = __ffma2_rd(dy01, rr, ct), ty23 = __ffma2_rd(dy23, rr, ct);
+        // bucket = min(bits(t) - bits(2^23), bins - 1) as unsigned: any input
+        // (also one outside the interval) stays inside the histogram
         const uint32_t top = (uint32_t)(bins - 1);
-        b0 = (int)(min((ux0 >> FX_FRAC) - kb, top) * (uint32_t)bins + min((uy0 >> FX_FRAC) - kb, top));
-        b1 = (int)(min((ux1 >> FX_FRAC) - kb, top) * (uint32_t)bins + min((uy1 >> FX_FRAC) - kb, top));
-        b2 = (int)(min((ux2 >> FX_FRAC) - kb, top) * (uint32_t)bins + min((uy2 >> FX_FRAC) - kb, top));
-        b3 = (int)(min((ux3 >> FX_FRAC) - kb, top) * (uint32_t)bins + min((uy3 >> FX_FRAC) - kb, top));
+        const uint32_t ub = (uint32_t)bins;
+        b0 = (int)(min(__float_as_uint(tx01.x) - FLOOR_BASE_BITS, top) * ub +
+                   min(__float_as_uint(ty01.x) - FLOOR_BASE_BITS, top));
+        b1 = (int)(min(__float_as_uint(tx01.y) - FLOOR_BASE_BITS, top) * ub +
+                   min(__float_as_uint(ty01.y) - FLOOR_BASE_BITS, top));
+        b2 = (int)(min(__float_as_uint(tx23.x) - FLOOR_BASE_BITS, top) * ub +
+                   min(__float_as_uint(ty23.x) - FLOOR_BASE_BITS, top));
+        b3 = (int)(min(__float_as_uint(tx23.y) - FLOOR_BASE_BITS, top) * ub +
+                   min(__float_as_uint(ty23.y) - FLOOR_BASE_BITS, top));
         // Ambiguous values: u = bits(1536) | w with w a nonzero multiple of
         // 2^13, i.e. the lowest set bit of u lies in bits 13..21 (for w = 0
         // the lowest set bit is bit 22 of bits(1536)).  u & (2^29 - u) keeps

@@ -59,6 +59,24 @@ def fixed_point_bucket(v, mn, step, bins):
     return bucket, ambiguous
 
 
+def floor_bucket(v, mn, step, bins):
+    """The kernels' bucket: RD(RN(v - mn) * RN(1/step) + 2^23) - 2^23 = the
+    floor of the exact product, clamped to bins - 1 (exact integer emulation)."""
+    r = np.float32(1.0) / np.float32(step)
+    d = (v - mn).astype(np.float32)
+    md, ed = _significand(d)
+    mr, er = _significand(np.full_like(d, r))
+    prod = md * mr
+    sh = ed + er
+    fl = np.zeros_like(prod)
+    up = sh >= 0
+    fl[up] = prod[up] << sh[up]
+    k = np.clip(-sh, 0, 62)
+    dn = (~up) & (-sh <= 62)
+    fl[dn] = (prod >> k)[dn]
+    return np.minimum(fl, bins - 1)
+
+
 def intervals(rng, count):
     out = []
     for _ in range(count):
@@ -101,6 +119,8 @@ def test_fast_path_agrees_with_division(bins):
         fx, amb = fixed_point_bucket(vals, mn, step, bins)
         ok = ~amb
         assert np.array_equal(fx[ok], ref[ok]), (mn, mx, bins)
+        # the bucket the kernels count (floor of the exact product) agrees too
+        assert np.array_equal(floor_bucket(vals, mn, step, bins)[ok], ref[ok]), (mn, mx, bins)
         kept += int(ok.sum())
         flagged += int(amb.sum())
         # v == mn (q = 0) stays on the fast path
