@@ -328,7 +328,7 @@ __device__ __forceinline__ float2 child_dist2(const Query &q, const float4 &a, c
 constexpr int PATCH_Z = 8, PATCH_Y = 4, WARPS_Y = QUERY_THREADS / 32;
 // samples per lane along x: long runs amortise the first pair's greedy bound;
 // short runs keep enough blocks in flight for small volumes
-constexpr int RUN_X_LONG = 32, RUN_X_SHORT = 8;
+constexpr int RUN_X_LONG = 64, RUN_X_SHORT = 8;
 constexpr int QUERY_GROUP = 4;  // samples per lane traversed together
 
 __device__ __forceinline__ void load_node(const BvhNode *nodes, int cur, float4 &a, float4 &b, float4 &c, int4 &d)
