@@ -700,11 +700,12 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_seg_kernel(Se
         uint32_t *gh = a.ghist + (size_t)p * bins * bins;
         const int64_t v0 = (int64_t)seg * a.seg_len;
         const int64_t v1 = v0 + a.seg_len < a.n ? v0 + a.seg_len : a.n;
-        const float *f1 = a.fa + (size_t)i * a.stride;
-        const float *f2 = a.fb + (size_t)j * a.stride;
+        // the segment as a range of its own (same loop code as one pair per CTA)
+        const float *f1 = a.fa + (size_t)i * a.stride + v0;
+        const float *f2 = a.fb + (size_t)j * a.stride + v0;
         const Counter<GlobalWrap> cnt{words, GlobalWrap{gh}};
-        if (bn.mode == 0) stream_values<0>(bn, f1, f2, v0, v1, cnt);
-        else stream_values<1>(bn, f1, f2, v0, v1, cnt);
+        if (bn.mode == 0) stream_values<0>(bn, f1, f2, 0, v1 - v0, cnt);
+        else stream_values<1>(bn, f1, f2, 0, v1 - v0, cnt);
         __syncthreads();
         for (int w = threadIdx.x; w < nwords; w += blockDim.x) {
             const uint32_t val = words[w];
