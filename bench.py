@@ -529,8 +529,7 @@ def run_multi(args):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ctx.pair_map(fields, pairs, bins=bins, n=F, stride=stride, out=pmap)
-        vals = pmap[torch.from_numpy(pairs[:, 0]).long().cuda(), torch.from_numpy(pairs[:, 1]).long().cuda()]
-        out = vals.cpu().numpy()
+        out = pmap.cpu().numpy()[pairs[:, 0], pairs[:, 1]]
         stats["t_cross"] = time.perf_counter() - t0
         stats["cross_pairs"] = len(pairs)
         return out

@@ -39,15 +39,17 @@ def shard(count, rank, world):
 
 
 def block_pairs(blocks, reps):
-    """Field pairs (rows of the representative matrix) of each volume block."""
-    out = np.empty((len(blocks) * reps * reps, 2), dtype=np.int32)
-    q = 0
-    for a, b in blocks:
-        for i in range(reps):
-            for j in range(reps):
-                out[q] = (a * reps + i, b * reps + j)
-                q += 1
-    return out
+    """Field pairs (rows of the representative matrix) of each volume block:
+    block (a, b) gives (a*reps + i, b*reps + j) for i, j in [0, reps), i major."""
+    if len(blocks) == 0:
+        return np.empty((0, 2), dtype=np.int32)
+    bl = np.asarray(blocks, dtype=np.int64).reshape(-1, 1, 1, 2)
+    i = np.arange(reps).reshape(1, reps, 1)
+    j = np.arange(reps).reshape(1, 1, reps)
+    out = np.empty((len(blocks), reps, reps, 2), dtype=np.int32)
+    out[..., 0] = bl[..., 0] * reps + i
+    out[..., 1] = bl[..., 1] * reps + j
+    return out.reshape(-1, 2)
 
 
 def run_batch(dist, rank, world, variables, timesteps, reps, local_fields_fn, pair_map_fn):
