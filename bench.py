@@ -216,17 +216,14 @@ def run_ours(args):
     achieved = hist_bytes / hist_s / 1e9
     counter_peak = ctx.counter_rate(bins if bins & (bins - 1) == 0 else 256)
     updates = F * pairs / hist_s
-    # DRAM traffic of the histogram stage: --hist-traffic, else one-pass ncu
-    # captures (dram__bytes_read.sum + dram__bytes_write.sum) of the default
-    # 256^3 workload: the segment-major schedule (8 chunks: 8 segment-kernel
-    # and 8 NMI-kernel launches, summed) or the one-CTA-per-pair kernel
+    # DRAM traffic of the histogram stage: --hist-traffic, else a one-pass ncu
+    # capture (dram__bytes_read.sum + dram__bytes_write.sum) of the default
+    # 256^3 workload with the segment-major schedule (9 chunks: 9 segment-kernel
+    # and 9 NMI-kernel launches, summed); other schedules report null
     traffic, traffic_src = args.hist_traffic, "--hist-traffic"
-    if traffic is None and args.config == 3 and bins == 256:
-        if seg_values == 2097152:
-            traffic = 1.4799e12 + 12.25e9 + 8.613e9 + 2.6e6
-            traffic_src = "ncu capture of this workload (16 launches of the stage, 517 ms)"
-        elif seg_values == 0:
-            traffic, traffic_src = 2.80e12 + 35.7e6, "ncu capture of this workload (one launch, 533.4 ms)"
+    if traffic is None and args.config == 3 and bins == 256 and seg_values == 2097152:
+        traffic = 7.9575e11 + 11.372e9 + 8.6476e9 + 1.8e6
+        traffic_src = "ncu capture of this workload (18 launches of the stage, 431 ms)"
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 5), "traffic": traffic,
                 "traffic_source": traffic_src if traffic is not None else None,

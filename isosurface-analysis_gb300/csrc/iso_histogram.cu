@@ -8,9 +8,10 @@
 //
 // Kernels: persistent CTAs pull unordered pair tasks (i <= j) from a counter and
 // stream both fields with 128-bit loads.  Each voxel's two buckets (the
-// reference's binning: a fixed-point reciprocal, exact IEEE division where the
-// reciprocal cannot decide) form one bin, counted in shared memory as a 16-bit
-// half of a 32-bit word (bins*bins/2 words: 128 KB at 256 bins).  A half that
+// reference's binning: floors of the products with two widened reciprocals,
+// exact IEEE division where they disagree) form one bin, counted in shared
+// memory as a 16-bit half of a 32-bit word (rows of bins/2 words plus 3 pad
+// words: 131 KB at 256 bins).  A half that
 // wraps is seen by the thread whose atomic returned 0xFFFF, which records the
 // exact correction.  Short fields: one CTA per pair, FP64 NMI in the same CTA
 // (joint_histogram_mi_kernel).  Long fields: (segment, pair) tasks add into
@@ -26,6 +27,24 @@
 namespace {
 
 constexpr int HIST_THREADS = 1024;
+
+// Shared histograms pad every row, so that the same column of rows r and r + 1
+// lies in different banks.  Without it a row of 256 packed counters (128
+// words) or of 32 * k 32-bit counters starts in the same bank as the row
+// before, and the atomics of a warp whose voxels differ only in their row bin
+// (common for two similar fields) all hit one bank.
+//   packed 16-bit counters: counter index row * (bins + 2 * PACKED_PAD) + col,
+//                           word = index / 2 (PACKED_PAD pad words per row)
+//   32-bit counters:        counter index row * (bins + 1) + col
+// Three pad words rather than one: 4 % fewer shared-memory wavefronts per
+// atomic on the distance fields of a 128^3 volume (a CPU model of the bank
+// conflicts over 28 field pairs: 4.88 unpadded, 3.54 with one, 3.39 with three).
+constexpr int PACKED_PAD = 3;
+__host__ __device__ constexpr int packed_stride(int bins) { return bins + 2 * PACKED_PAD; }
+__host__ __device__ constexpr int packed_row_words(int bins) { return bins / 2 + PACKED_PAD; }
+__host__ __device__ constexpr int packed_words(int bins) { return bins * (bins / 2 + PACKED_PAD); }
+__host__ __device__ constexpr int wide_stride(int bins) { return bins + 1; }
+__host__ __device__ constexpr int wide_words(int bins) { return bins * (bins + 1); }
 
 __device__ __forceinline__ float bits_to_float(uint32_t b) { return __uint_as_float(b); }
 
@@ -52,9 +71,11 @@ struct PairArgs {
 };
 
 struct Binner {
-    float mn, step, r;
+    float mn, step;
+    float rlo, rhi;  // RN(1/step) widened down and up (mode 0)
     int bins;
-    int mode;  // 0: fixed-point reciprocal with exact fallback, 1: exact division only, 2: step == 0
+    int rstride;     // counter index of (row, col) = row * rstride + col (padded rows)
+    int mode;  // 0: bracketed reciprocal with exact fallback, 1: exact division only, 2: step == 0
 };
 
 
@@ -64,91 +85,90 @@ __device__ __forceinline__ int exact_bucket(const Binner &b, float v) { return i
 
 // Bins of four voxels by IEEE division.  Out of line: the exact path is rare
 // in mode 0 and would otherwise cost registers in the streaming loop.
-__device__ __noinline__ int4 exact_bins4(float mn, float step, int bins, float4 x, float4 y)
+__device__ __noinline__ int4 exact_bins4(float mn, float step, int bins, int rs, float4 x, float4 y)
 {
-    return make_int4(iso_bucket(x.x, mn, step, bins) * bins + iso_bucket(y.x, mn, step, bins),
-                     iso_bucket(x.y, mn, step, bins) * bins + iso_bucket(y.y, mn, step, bins),
-                     iso_bucket(x.z, mn, step, bins) * bins + iso_bucket(y.z, mn, step, bins),
-                     iso_bucket(x.w, mn, step, bins) * bins + iso_bucket(y.w, mn, step, bins));
+    return make_int4(iso_bucket(x.x, mn, step, bins) * rs + iso_bucket(y.x, mn, step, bins),
+                     iso_bucket(x.y, mn, step, bins) * rs + iso_bucket(y.y, mn, step, bins),
+                     iso_bucket(x.z, mn, step, bins) * rs + iso_bucket(y.z, mn, step, bins),
+                     iso_bucket(x.w, mn, step, bins) * rs + iso_bucket(y.w, mn, step, bins));
 }
 
-// ---- fixed-point bucket ----------------------------------------------------
-// With d = RN(v - mn) and r = RN(1/step), two packed FMAs per two values:
-//   t = RD(d * r + 2^23) = 2^23 + floor(d * r) (ulp 1 in [2^23, 2^24)), so the
-//     bucket candidate floor(d * r) is the low mantissa bits of t;
-//   s = RN(d * r + 1536): 1536 = 1.5 * 2^10, so s lies in [1536, 2048) where
-//     the float ulp is 2^-13: u = bits(s) - bits(1536) is d * r rounded to a
-//     fixed-point number with 13 fraction bits.
-// d * r differs from the reference's quotient q = RN(d / step) by less than
-// q * 2^-24 (r) + 2^-17 (rounding of q, q < 256) < 2^-15, so floor(d * r) =
-// floor(q) unless d * r lies within 2^-15 of a nonzero integer, and then s
-// (within 2^-14 of d * r) is that integer: values whose s is a nonzero
-// integer (u a nonzero multiple of 2^13) take the division.  u = 0 means
-// d * r < 2^-14, where both floors are 0.  Near q = bins both sides clamp to
-// the last bucket, so that boundary needs no check.
-constexpr float FX_BASE = 1536.0f;
+// ---- bracketed floor bucket ----------------------------------------------
+// With d = RN(v - mn) >= 0, r = RN(1/step), rlo = RD(r * (1 - 2^-22)) and
+// rhi = RU(r * (1 + 2^-22)): r lies within a relative 2^-24 of 1/step and the
+// reference's quotient q = RN(d / step) within a relative 2^-24 of d / step,
+// so d * rlo <= q <= d * rhi and floor(d * rlo) <= floor(q) <= floor(d * rhi).
+// Two packed FMAs give both floors exactly:
+//   lo = RD(d * rlo + 2^23)   = 2^23 + floor(d * rlo)  (ulp 1 in [2^23, 2^24)),
+//   hi = RU(d * -rhi - 2^23)  = -(2^23 + floor(d * rhi)),
+// and lo + hi = floor(d * rlo) - floor(d * rhi) <= 0 is exact.  Where it is 0
+// the bucket is bits(lo) - bits(2^23).  The sum of lo + hi over the eight
+// values of four voxels is 0 exactly when every pair of floors agrees; a NaN
+// value makes it NaN.  Either way the four voxels take the division, which
+// happens for about 2^-20 * q of the values.  Near q = bins the bucket is
+// clamped to the last bin on both paths.
 constexpr float FLOOR_BASE = 8388608.0f;  // 2^23
 constexpr uint32_t FLOOR_BASE_BITS = 0x4B000000u;
 
-// Bins (row = field-1 bucket, column = field-2 bucket) of the four voxels in x, y.
-template <int MODE>
-__device__ __forceinline__ void bins4(const Binner &bn, const float4 &x, const float4 &y, int &b0, int &b1, int &b2,
-                                      int &b3)
+// The same four voxels, loaded again from p1[q], p2[q]: the rare exact path
+// reloads them, so the streaming loop does not keep x and y alive across the
+// bucket arithmetic.
+__device__ __noinline__ int4 exact_bins4_at(float mn, float step, int bins, int rs, const float4 *p1, const float4 *p2,
+                                            int q)
 {
-    const int bins = bn.bins;
+    return exact_bins4(mn, step, bins, rs, __ldg(p1 + q), __ldg(p2 + q));
+}
+
+// Bins (row = field-1 bucket, column = field-2 bucket) of the four voxels in
+// x = p1[q], y = p2[q].  FB / FRS: bins and row stride as compile-time
+// constants (0: read from the binner), which keeps them out of registers in
+// the streaming loop.  RELOAD: the exact path loads the voxels again instead
+// of keeping x and y.
+template <int MODE, int FB, int FRS, bool RELOAD>
+__device__ __forceinline__ void bins4(const Binner &bn, const float4 &x, const float4 &y, const float4 *p1,
+                                      const float4 *p2, int q, int &b0, int &b1, int &b2, int &b3)
+{
+    const int bins = FB ? FB : bn.bins;
+    const int rstride = FRS ? FRS : bn.rstride;
     if (MODE == 0) {
-        const float2 nm = make_float2(-bn.mn, -bn.mn), rr = make_float2(bn.r, bn.r);
+        const float2 nm = make_float2(-bn.mn, -bn.mn);
+        const float2 rl = make_float2(bn.rlo, bn.rlo), nrh = make_float2(-bn.rhi, -bn.rhi);
+        const float2 pb = make_float2(FLOOR_BASE, FLOOR_BASE), nb = make_float2(-FLOOR_BASE, -FLOOR_BASE);
         const float2 dx01 = __fadd2_rn(make_float2(x.x, x.y), nm), dx23 = __fadd2_rn(make_float2(x.z, x.w), nm);
         const float2 dy01 = __fadd2_rn(make_float2(y.x, y.y), nm), dy23 = __fadd2_rn(make_float2(y.z, y.w), nm);
-        // s: the quotient on the 2^-13 grid (for the ambiguity test below)
-        const float2 cs = make_float2(FX_BASE, FX_BASE);
-        const float2 sx01 = __ffma2_rn(dx01, rr, cs), sx23 = __ffma2_rn(dx23, rr, cs);
-        const float2 sy01 = __ffma2_rn(dy01, rr, cs), sy23 = __ffma2_rn(dy23, rr, cs);
-        const uint32_t ux0 = __float_as_uint(sx01.x), ux1 = __float_as_uint(sx01.y);
-        const uint32_t ux2 = __float_as_uint(sx23.x), ux3 = __float_as_uint(sx23.y);
-        const uint32_t uy0 = __float_as_uint(sy01.x), uy1 = __float_as_uint(sy01.y);
-        const uint32_t uy2 = __float_as_uint(sy23.x), uy3 = __float_as_uint(sy23.y);
-        // t = RD(d * r + 2^23) = 2^23 + floor(d * r): the bucket is its low
-        // mantissa bits, with no shift.  floor(d * r) equals the reference's
-        // bucket except where s is ambiguous (within 2^-14 of an integer
-        // covers the 2^-15 between d * r and the reference's quotient).
-        const float2 ct = make_float2(FLOOR_BASE, FLOOR_BASE);
-        const float2 tx01 = __ffma2_rd(dx01, rr, ct), tx23 = __ffma2_rd(dx23, rr, ct);
-        const float2 ty01 = __ffma2_rd(dy01, rr, ct), ty23 = __ffma2_rd(dy23, rr, ct);
-        // bucket = min(bits(t) - bits(2^23), bins - 1) as unsigned: any input
+        const float2 lx01 = __ffma2_rd(dx01, rl, pb), lx23 = __ffma2_rd(dx23, rl, pb);
+        const float2 ly01 = __ffma2_rd(dy01, rl, pb), ly23 = __ffma2_rd(dy23, rl, pb);
+        const float2 hx01 = __ffma2_ru(dx01, nrh, nb), hx23 = __ffma2_ru(dx23, nrh, nb);
+        const float2 hy01 = __ffma2_ru(dy01, nrh, nb), hy23 = __ffma2_ru(dy23, nrh, nb);
+        const float2 zx = __fadd2_rn(__fadd2_rn(lx01, hx01), __fadd2_rn(lx23, hx23));
+        const float2 zy = __fadd2_rn(__fadd2_rn(ly01, hy01), __fadd2_rn(ly23, hy23));
+        const float2 z = __fadd2_rn(zx, zy);
+        // bucket = min(bits(lo) - bits(2^23), bins - 1) as unsigned: any input
         // (also one outside the interval) stays inside the histogram
         const uint32_t top = (uint32_t)(bins - 1);
-        const uint32_t ub = (uint32_t)bins;
-        b0 = (int)(min(__float_as_uint(tx01.x) - FLOOR_BASE_BITS, top) * ub +
-                   min(__float_as_uint(ty01.x) - FLOOR_BASE_BITS, top));
-        b1 = (int)(min(__float_as_uint(tx01.y) - FLOOR_BASE_BITS, top) * ub +
-                   min(__float_as_uint(ty01.y) - FLOOR_BASE_BITS, top));
-        b2 = (int)(min(__float_as_uint(tx23.x) - FLOOR_BASE_BITS, top) * ub +
-                   min(__float_as_uint(ty23.x) - FLOOR_BASE_BITS, top));
-        b3 = (int)(min(__float_as_uint(tx23.y) - FLOOR_BASE_BITS, top) * ub +
-                   min(__float_as_uint(ty23.y) - FLOOR_BASE_BITS, top));
-        // Ambiguous values: u = bits(1536) | w with w a nonzero multiple of
-        // 2^13, i.e. the lowest set bit of u lies in bits 13..21 (for w = 0
-        // the lowest set bit is bit 22 of bits(1536)).  u & (2^29 - u) keeps
-        // that lowest bit (2^29 - u equals -u below bit 29) and adds bit 29 for
-        // a NaN (exponent bits all set), which in-range values never have.  One
-        // OR over the eight values tests them all; both kinds take the division.
-        constexpr uint32_t B29 = 0x20000000u;
-        const uint32_t low = (ux0 & (B29 - ux0)) | (ux1 & (B29 - ux1)) | (ux2 & (B29 - ux2)) | (ux3 & (B29 - ux3)) |
-                             (uy0 & (B29 - uy0)) | (uy1 & (B29 - uy1)) | (uy2 & (B29 - uy2)) | (uy3 & (B29 - uy3));
-        const bool slow = (low & 0x203FE000u) != 0u;
+        const uint32_t ub = (uint32_t)rstride;
+        b0 = (int)(min(__float_as_uint(lx01.x) - FLOOR_BASE_BITS, top) * ub +
+                   min(__float_as_uint(ly01.x) - FLOOR_BASE_BITS, top));
+        b1 = (int)(min(__float_as_uint(lx01.y) - FLOOR_BASE_BITS, top) * ub +
+                   min(__float_as_uint(ly01.y) - FLOOR_BASE_BITS, top));
+        b2 = (int)(min(__float_as_uint(lx23.x) - FLOOR_BASE_BITS, top) * ub +
+                   min(__float_as_uint(ly23.x) - FLOOR_BASE_BITS, top));
+        b3 = (int)(min(__float_as_uint(lx23.y) - FLOOR_BASE_BITS, top) * ub +
+                   min(__float_as_uint(ly23.y) - FLOOR_BASE_BITS, top));
+        const bool slow = !(__fadd_rn(z.x, z.y) == 0.0f);
         if (__builtin_expect(slow, 0)) {
-            const int4 e = exact_bins4(bn.mn, bn.step, bins, x, y);
+            const int4 e = RELOAD ? exact_bins4_at(bn.mn, bn.step, bins, rstride, p1, p2, q)
+                                  : exact_bins4(bn.mn, bn.step, bins, rstride, x, y);
             b0 = e.x;
             b1 = e.y;
             b2 = e.z;
             b3 = e.w;
         }
     } else {
-        b0 = exact_bucket(bn, x.x) * bins + exact_bucket(bn, y.x);
-        b1 = exact_bucket(bn, x.y) * bins + exact_bucket(bn, y.y);
-        b2 = exact_bucket(bn, x.z) * bins + exact_bucket(bn, y.z);
-        b3 = exact_bucket(bn, x.w) * bins + exact_bucket(bn, y.w);
+        b0 = exact_bucket(bn, x.x) * rstride + exact_bucket(bn, y.x);
+        b1 = exact_bucket(bn, x.y) * rstride + exact_bucket(bn, y.y);
+        b2 = exact_bucket(bn, x.z) * rstride + exact_bucket(bn, y.z);
+        b3 = exact_bucket(bn, x.w) * rstride + exact_bucket(bn, y.w);
     }
 }
 
@@ -217,16 +237,19 @@ __device__ __forceinline__ double clnc_of(const double *table, unsigned long lon
 }
 
 // Streams values [v0, v1) of one field pair (v0 a multiple of 4, rows 16-byte
-// aligned) into a shared histogram through count.add4 / count.add1.  Two load pairs alternate so that one is in
-// flight while the other is binned.
-template <int MODE, class Count>
+// aligned) into a shared histogram through count.add4 / count.add1.  Two load
+// pairs alternate so that one is in flight while the other is binned.  Blocks
+// of HIST_THREADS threads; CSTEP: that block size as a constant instead of
+// blockDim.x (the compiler's register allocation in this loop, and with it the
+// kernel's speed, depends on the choice: each kernel uses the faster one).
+template <int MODE, int FB, int FRS, bool CSTEP, bool RELOAD, class Count>
 __device__ __forceinline__ void stream_values(const Binner &bn, const float *f1, const float *f2, int64_t v0,
                                               int64_t v1, const Count &count)
 {
     const float4 *p1 = reinterpret_cast<const float4 *>(f1 + v0);
     const float4 *p2 = reinterpret_cast<const float4 *>(f2 + v0);
     const int n4 = (int)((v1 - v0) >> 2);
-    const int step = (int)blockDim.x;
+    const int step = CSTEP ? HIST_THREADS : (int)blockDim.x;
     int q = (int)threadIdx.x;
     float4 xa = make_float4(0.f, 0.f, 0.f, 0.f), ya = xa, xb = xa, yb = xa;
     if (q < n4) {
@@ -240,7 +263,7 @@ __device__ __forceinline__ void stream_values(const Binner &bn, const float *f1,
             yb = __ldg(p2 + qb);
         }
         int c0, c1, c2, c3;
-        bins4<MODE>(bn, xa, ya, c0, c1, c2, c3);
+        bins4<MODE, FB, FRS, RELOAD>(bn, xa, ya, p1, p2, q, c0, c1, c2, c3);
         count.add4(c0, c1, c2, c3);
         if (qb >= n4) break;
         const int qa = qb + step;
@@ -248,12 +271,12 @@ __device__ __forceinline__ void stream_values(const Binner &bn, const float *f1,
             xa = __ldg(p1 + qa);
             ya = __ldg(p2 + qa);
         }
-        bins4<MODE>(bn, xb, yb, c0, c1, c2, c3);
+        bins4<MODE, FB, FRS, RELOAD>(bn, xb, yb, p1, p2, qb, c0, c1, c2, c3);
         count.add4(c0, c1, c2, c3);
         q = qa;
     }
-    for (int64_t v = v0 + ((int64_t)n4 << 2) + threadIdx.x; v < v1; v += blockDim.x) {
-        const int bin = bn.mode == 2 ? 0 : exact_bucket(bn, f1[v]) * bn.bins + exact_bucket(bn, f2[v]);
+    for (int64_t v = v0 + ((int64_t)n4 << 2) + threadIdx.x; v < v1; v += step) {
+        const int bin = bn.mode == 2 ? 0 : exact_bucket(bn, f1[v]) * bn.rstride + exact_bucket(bn, f2[v]);
         count.add1(bin);
     }
 }
@@ -296,25 +319,33 @@ struct WideCounter {
 
 // Interval of one pair: the union of both fields' intervals; step, reciprocal
 // and the bucket mode (JointHistogram.cu:100-120).
-__device__ __forceinline__ Binner make_binner(const uint32_t *mma, const uint32_t *mmb, int i, int j, int bins)
+__device__ __forceinline__ Binner make_binner(const uint32_t *mma, const uint32_t *mmb, int i, int j, int bins,
+                                              int rstride)
 {
     Binner bn;
+    bn.rstride = rstride;
     const float mn_i = bits_to_float(mma[2 * i]), mx_i = bits_to_float(mma[2 * i + 1]);
     const float mn_j = bits_to_float(mmb[2 * j]), mx_j = bits_to_float(mmb[2 * j + 1]);
     bn.mn = mn_i < mn_j ? mn_i : mn_j;
     const float mx = mx_i > mx_j ? mx_i : mx_j;
     bn.step = __fdiv_rn(__fsub_rn(mx, bn.mn), (float)bins);
     bn.bins = bins;
-    bn.r = __frcp_rn(bn.step);
+    const float r = __frcp_rn(bn.step);
+    bn.rlo = __fmul_rd(r, 0.99999976158142089844f);  // 1 - 2^-22
+    bn.rhi = __fmul_ru(r, 1.00000023841857910156f);  // 1 + 2^-22
     // mode 0 needs a finite interval (every non-NaN value then lies in it) and
-    // a normal, finite step with a finite nonzero reciprocal
+    // a normal, finite step with finite nonzero reciprocals
     bn.mode = bn.step == 0.0f ? 2
-              : (isfinite(bn.step) && bn.step >= 1.17549435e-38f && isfinite(bn.r) && bn.r > 0.0f ? 0 : 1);
+              : (isfinite(bn.step) && bn.step >= 1.17549435e-38f && isfinite(r) && r > 0.0f && isfinite(bn.rhi)
+                     ? 0
+                     : 1);
     return bn;
 }
 
+template <int FB, bool CSTEP, bool RELOAD>
 __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(PairArgs a)
 {
+    constexpr int FRS = FB ? packed_stride(FB) : 0;
     extern __shared__ uint32_t words[];
     __shared__ int s_task;
     __shared__ unsigned int s_nev;
@@ -323,8 +354,10 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
     __shared__ uint32_t s_rowsum[ISO_MAX_BINS];
 
     const int bins = a.bins;
-    const int nwords = bins * bins / 2;
-    const int wpr = bins / 2;  // words per histogram row
+    const int nwords = packed_words(bins);
+    const int wpr = bins / 2;                   // counter words per histogram row
+    const int wps = packed_row_words(bins);     // words per padded row
+    const int rs = packed_stride(bins);
     int4 *ev = a.events + (size_t)blockIdx.x * a.event_cap;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
 
@@ -345,15 +378,15 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
         const int2 task = a.tasks[t];
         const int i = task.x, j = task.y;
 
-        const Binner bn = make_binner(a.mma, a.mmb, i, j, bins);
+        const Binner bn = make_binner(a.mma, a.mmb, i, j, bins, rs);
 
         const float *f1 = a.fa + (size_t)i * a.stride;
         const float *f2 = a.fb + (size_t)j * a.stride;
 
         // streaming loop, one load pair in flight ahead of the one being binned
         const Counter<EventWrap> cnt{words, EventWrap{ev, a.event_cap, &s_nev, a.error}};
-        if (bn.mode == 0) stream_values<0>(bn, f1, f2, 0, a.n, cnt);
-        else stream_values<1>(bn, f1, f2, 0, a.n, cnt);
+        if (bn.mode == 0) stream_values<0, FB, FRS, CSTEP, RELOAD>(bn, f1, f2, 0, a.n, cnt);
+        else stream_values<1, FB, FRS, CSTEP, RELOAD>(bn, f1, f2, 0, a.n, cnt);
         __syncthreads();
 
         // ---- wrap corrections: per distinct bin, total correction and its
@@ -377,8 +410,8 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
             const uint32_t c16 = (words[bin >> 1] >> ((bin & 1) << 4)) & 0xffffu;
             const unsigned long long ctrue = (unsigned long long)((long long)c16 + corr);
             hxy -= clnc_of(a.clnc, ctrue) - clnc_of(a.clnc, c16);
-            atomicAdd(&s_rowsum[bin / bins], (uint32_t)corr);  // modular: corr may be negative
-            atomicAdd(&s_colsum[bin % bins], (uint32_t)corr);
+            atomicAdd(&s_rowsum[bin / rs], (uint32_t)corr);  // modular: corr may be negative
+            atomicAdd(&s_colsum[bin % rs], (uint32_t)corr);
             ev[e].z = (int)c16;
             ev[e].w = (int)ctrue;  // only read back for histogram dumps
         }
@@ -396,10 +429,10 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
             if (g < groups) {
                 uint32_t cs0 = 0, cs1 = 0;
                 for (int r = g; r < bins; r += groups) {
-                    const uint32_t word = words[r * wpr + w];
+                    const uint32_t word = words[r * wps + w];
                     uint32_t c0 = 0, c1 = 0;
                     if (word || dump) {
-                        words[r * wpr + w] = 0;
+                        words[r * wps + w] = 0;
                         c0 = word & 0xffffu;
                         c1 = word >> 16;
                         cs0 += c0;
@@ -439,7 +472,7 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
                         break;
                     }
                 if (!first) continue;
-                const int r = bin / bins, c = bin % bins;
+                const int r = bin / rs, c = bin % rs;
                 const uint32_t val = (uint32_t)ev[e].w;
                 a.joint_dump[(((size_t)i * a.m + j) * bins + r) * bins + c] = val;
                 if (a.symmetric && i != j) a.joint_dump[(((size_t)j * a.m + i) * bins + c) * bins + r] = val;
@@ -506,8 +539,10 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
 
 constexpr int WIDE_MAX_BINS = ISO_WIDE_MAX_BINS;
 
+template <int FB>
 __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_wide_kernel(PairArgs a)
 {
+    constexpr int FRS = FB ? wide_stride(FB) : 0;
     extern __shared__ uint32_t words[];
     __shared__ int s_task;
     __shared__ double s_red[3][HIST_THREADS / 32];
@@ -521,7 +556,7 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_wide_kernel(P
     // of the block size as bins each thread reads one column
     const bool warp_rows = (bins & 31) == 0;
     const bool col_own = (blockDim.x % bins) == 0;
-    for (int w = threadIdx.x; w < nb; w += blockDim.x) words[w] = 0;
+    for (int w = threadIdx.x; w < wide_words(bins); w += blockDim.x) words[w] = 0;
 
     for (;;) {
         if (threadIdx.x == 0) s_task = (int)atomicAdd(a.counter, 1u);
@@ -534,12 +569,12 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_wide_kernel(P
         if (t >= a.num_tasks) break;
         const int2 task = a.tasks[t];
         const int i = task.x, j = task.y;
-        const Binner bn = make_binner(a.mma, a.mmb, i, j, bins);
+        const Binner bn = make_binner(a.mma, a.mmb, i, j, bins, wide_stride(bins));
         const float *f1 = a.fa + (size_t)i * a.stride;
         const float *f2 = a.fb + (size_t)j * a.stride;
         const WideCounter cnt{words};
-        if (bn.mode == 0) stream_values<0>(bn, f1, f2, 0, a.n, cnt);
-        else stream_values<1>(bn, f1, f2, 0, a.n, cnt);
+        if (bn.mode == 0) stream_values<0, FB, FRS, false, true>(bn, f1, f2, 0, a.n, cnt);
+        else stream_values<1, FB, FRS, false, true>(bn, f1, f2, 0, a.n, cnt);
         __syncthreads();
 
         // bins: sum(c ln c), marginals, optional dump; clears the counters
@@ -547,10 +582,10 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_wide_kernel(P
         double hxy = 0.0;
         uint32_t cs = 0;
         for (int idx = threadIdx.x; idx < nb; idx += blockDim.x) {
-            const uint32_t c = words[idx];
             const int r = idx / bins, col = idx - r * bins;
+            const uint32_t c = words[idx + r];  // padded row r starts at r * (bins + 1)
             if (c) {
-                words[idx] = 0;
+                words[idx + r] = 0;
                 hxy -= clnc_of(a.clnc, c);
             }
             if (dump) {
@@ -656,21 +691,27 @@ __device__ __noinline__ void log_wrap_global(uint32_t *gh, int bin, uint32_t odd
     }
 }
 
-// Wraps corrected straight in the pair's global histogram (segment-major kernel).
+// Wraps corrected straight in the pair's global histogram (segment-major
+// kernel).  The global histogram is unpadded: shared counter index
+// row * packed_stride(bins) + col is global index row * bins + col (same parity).
 struct GlobalWrap {
     uint32_t *gh;
+    int rs;  // packed_stride(bins)
     __device__ __forceinline__ void operator()(int bin, uint32_t odd, uint32_t old) const
     {
-        log_wrap_global(gh, bin, odd, old);
+        log_wrap_global(gh, bin - 2 * PACKED_PAD * (bin / rs), odd, old);
     }
 };
 
+template <int FB, bool CSTEP, bool RELOAD>
 __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_seg_kernel(SegArgs a)
 {
+    constexpr int FRS = FB ? packed_stride(FB) : 0;
     extern __shared__ uint32_t words[];
     __shared__ int s_task;
     const int bins = a.bins;
-    const int nwords = bins * bins / 2;
+    const int nwords = packed_words(bins);
+    const int wps = packed_row_words(bins), rs = packed_stride(bins);
     for (int w = threadIdx.x; w < nwords; w += blockDim.x) words[w] = 0;
     const int total = a.num_pairs * a.num_segs;
     for (;;) {
@@ -696,23 +737,24 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_seg_kernel(Se
         }
         const int2 task = a.tasks[p];
         const int i = task.x, j = task.y;
-        const Binner bn = make_binner(a.mma, a.mmb, i, j, bins);
+        const Binner bn = make_binner(a.mma, a.mmb, i, j, bins, rs);
         uint32_t *gh = a.ghist + (size_t)p * bins * bins;
         const int64_t v0 = (int64_t)seg * a.seg_len;
         const int64_t v1 = v0 + a.seg_len < a.n ? v0 + a.seg_len : a.n;
         // the segment as a range of its own (same loop code as one pair per CTA)
         const float *f1 = a.fa + (size_t)i * a.stride + v0;
         const float *f2 = a.fb + (size_t)j * a.stride + v0;
-        const Counter<GlobalWrap> cnt{words, GlobalWrap{gh}};
-        if (bn.mode == 0) stream_values<0>(bn, f1, f2, 0, v1 - v0, cnt);
-        else stream_values<1>(bn, f1, f2, 0, v1 - v0, cnt);
+        const Counter<GlobalWrap> cnt{words, GlobalWrap{gh, rs}};
+        if (bn.mode == 0) stream_values<0, FB, FRS, CSTEP, RELOAD>(bn, f1, f2, 0, v1 - v0, cnt);
+        else stream_values<1, FB, FRS, CSTEP, RELOAD>(bn, f1, f2, 0, v1 - v0, cnt);
         __syncthreads();
         for (int w = threadIdx.x; w < nwords; w += blockDim.x) {
             const uint32_t val = words[w];
-            if (val) {
+            if (val) {  // the pad words stay 0
                 words[w] = 0;
-                if (val & 0xffffu) atomicAdd(&gh[2 * w], val & 0xffffu);
-                if (val >> 16) atomicAdd(&gh[2 * w + 1], val >> 16);
+                const int g = 2 * (w - PACKED_PAD * (w / wps));  // global index of the word's low counter
+                if (val & 0xffffu) atomicAdd(&gh[g], val & 0xffffu);
+                if (val >> 16) atomicAdd(&gh[g + 1], val >> 16);
             }
         }
         __syncthreads();
@@ -807,6 +849,23 @@ __global__ void __launch_bounds__(256) joint_mi_kernel(MiArgs a)
         a.ism[(size_t)i * a.m + j] = out;
         if (a.symmetric) a.ism[(size_t)j * a.m + i] = out;
     }
+}
+
+// The histogram kernels specialised for the common bin counts (bins and row
+// stride as constants in the streaming loop), else the generic instance.
+using PairKernel = void (*)(PairArgs);
+using SegKernel = void (*)(SegArgs);
+PairKernel mi_kernel_for(int bins)
+{
+    return bins == 256 ? joint_histogram_mi_kernel<256, false, false> : joint_histogram_mi_kernel<0, false, false>;
+}
+PairKernel wide_kernel_for(int bins)
+{
+    return bins == 128 ? joint_histogram_wide_kernel<128> : joint_histogram_wide_kernel<0>;
+}
+SegKernel seg_kernel_for(int bins)
+{
+    return bins == 256 ? joint_histogram_seg_kernel<256, true, true> : joint_histogram_seg_kernel<0, true, true>;
 }
 
 __global__ void clnc_table_kernel(double *table)
@@ -946,14 +1005,15 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
     }
     d_clnc = ctx->buf[BUF_CLNC];
 
-    const size_t smem = (size_t)bins * bins / 2 * sizeof(uint32_t);
+    const size_t smem = (size_t)packed_words(bins) * sizeof(uint32_t);
     const int64_t seg_len = ctx->hist_segment_values;
     if (seg_len > 0 && n > seg_len && bins > WIDE_MAX_BINS) {
         // long fields, packed counters: segment-major schedule, pairs in chunks
         // bounding the global histograms to ISO_HIST_CHUNK_BYTES (and the task
         // count to int range)
-        ISO_CUDA(cudaFuncSetAttribute(joint_histogram_seg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(ISO_MAX_BINS * ISO_MAX_BINS / 2 * sizeof(uint32_t))));
+        const SegKernel seg_kernel = seg_kernel_for(bins);
+        ISO_CUDA(cudaFuncSetAttribute(seg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(packed_words(ISO_MAX_BINS) * sizeof(uint32_t))));
         const size_t hist_bytes = (size_t)bins * bins * sizeof(uint32_t);
         const int64_t num_segs64 = (n + seg_len - 1) / seg_len;
         if (num_segs64 > (1 << 24)) return iso_fail(ISO_ERR_ARG, "histogram segments: %lld too many", (long long)num_segs64);
@@ -965,7 +1025,7 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
         void *d_gh;
         ISO_TRY(iso_buf(ctx, BUF_HIST_DUMP_SEG, (size_t)chunk * hist_bytes, &d_gh));
         int per_sm_seg = 0;
-        ISO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_seg, joint_histogram_seg_kernel, HIST_THREADS, smem));
+        ISO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_seg, seg_kernel, HIST_THREADS, smem));
         if (per_sm_seg < 1) per_sm_seg = 1;
         for (int c0 = 0; c0 < num_tasks; c0 += chunk) {
             const int np = std::min(chunk, num_tasks - c0);
@@ -988,7 +1048,7 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
             sa.counter = (unsigned int *)d_counter;
             const int64_t seg_tasks = (int64_t)np * num_segs;
             const int grid_seg = (int)std::min<int64_t>((int64_t)ctx->num_sms * per_sm_seg, seg_tasks);
-            joint_histogram_seg_kernel<<<grid_seg, HIST_THREADS, smem, ctx->stream>>>(sa);
+            seg_kernel<<<grid_seg, HIST_THREADS, smem, ctx->stream>>>(sa);
             ISO_LAUNCHED(ctx);
             MiArgs ma;
             ma.tasks = (const int2 *)d_tasks + c0;
@@ -1008,11 +1068,12 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
     }
     if (bins <= WIDE_MAX_BINS) {
         // 32-bit counters: no wrap events
-        const size_t wsmem = (size_t)bins * bins * sizeof(uint32_t);
-        ISO_CUDA(cudaFuncSetAttribute(joint_histogram_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(WIDE_MAX_BINS * WIDE_MAX_BINS * sizeof(uint32_t))));
+        const size_t wsmem = (size_t)wide_words(bins) * sizeof(uint32_t);
+        const PairKernel wide_kernel = wide_kernel_for(bins);
+        ISO_CUDA(cudaFuncSetAttribute(wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(wide_words(WIDE_MAX_BINS) * sizeof(uint32_t))));
         int per_sm_w = 0;
-        ISO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_w, joint_histogram_wide_kernel, HIST_THREADS,
+        ISO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_w, wide_kernel, HIST_THREADS,
                                                                wsmem));
         if (per_sm_w < 1) per_sm_w = 1;
         const int grid_w = std::min(ctx->num_sms * per_sm_w, num_tasks);
@@ -1036,14 +1097,15 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
         w.error = (int *)d_counter + 1;
         w.joint_dump = d_joint_dump;
         w.colrow_dump = d_colrow_dump;
-        joint_histogram_wide_kernel<<<grid_w, HIST_THREADS, wsmem, ctx->stream>>>(w);
+        wide_kernel<<<grid_w, HIST_THREADS, wsmem, ctx->stream>>>(w);
         ISO_LAUNCHED(ctx);
         return ISO_OK;
     }
-    ISO_CUDA(cudaFuncSetAttribute(joint_histogram_mi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(ISO_MAX_BINS * ISO_MAX_BINS / 2 * sizeof(uint32_t))));
+    const PairKernel mi_kernel = mi_kernel_for(bins);
+    ISO_CUDA(cudaFuncSetAttribute(mi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(packed_words(ISO_MAX_BINS) * sizeof(uint32_t))));
     int per_sm = 0;
-    ISO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, joint_histogram_mi_kernel, HIST_THREADS, smem));
+    ISO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mi_kernel, HIST_THREADS, smem));
     if (per_sm < 1) per_sm = 1;
     int grid = ctx->num_sms * per_sm;
     if (grid > num_tasks) grid = num_tasks;
@@ -1072,7 +1134,7 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
     a.error = (int *)d_counter + 1;
     a.joint_dump = d_joint_dump;
     a.colrow_dump = d_colrow_dump;
-    joint_histogram_mi_kernel<<<grid, HIST_THREADS, smem, ctx->stream>>>(a);
+    mi_kernel<<<grid, HIST_THREADS, smem, ctx->stream>>>(a);
     ISO_LAUNCHED(ctx);
     int err = 0;
     ISO_CUDA(cudaMemcpyAsync(&err, a.error, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1147,12 +1209,13 @@ int noalloc_setup(int device, NoAllocDevice **out)
         if (e != cudaSuccess)
             return iso_fail(ISO_ERR_CUDA, "iso_similarity_map_noalloc: cudaGetSymbolAddress failed: %s",
                             cudaGetErrorString(e));
-        ISO_CUDA(cudaFuncSetAttribute(joint_histogram_mi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(ISO_MAX_BINS * ISO_MAX_BINS / 2 * sizeof(uint32_t))));
+        for (int b : {0, 256})
+            ISO_CUDA(cudaFuncSetAttribute(mi_kernel_for(b), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)(packed_words(ISO_MAX_BINS) * sizeof(uint32_t))));
         int sms = 0, per_sm = 0;
         ISO_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-        ISO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, joint_histogram_mi_kernel, HIST_THREADS,
-                                                               ISO_MAX_BINS * ISO_MAX_BINS / 2 * sizeof(uint32_t)));
+        ISO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mi_kernel_for(0), HIST_THREADS,
+                                                               packed_words(ISO_MAX_BINS) * sizeof(uint32_t)));
         int grid = sms * (per_sm < 1 ? 1 : per_sm);
         d.grid = grid < NOALLOC_MAX_CTAS ? grid : NOALLOC_MAX_CTAS;
         clnc_table_kernel<<<256, 256>>>((double *)((unsigned char *)p + NA_OFF_CLNC));
@@ -1232,8 +1295,8 @@ extern "C" int iso_similarity_map_noalloc(const float *d_fields, int m, int64_t 
     a.joint_dump = nullptr;
     a.colrow_dump = nullptr;
     const int grid = d->grid < num_tasks ? d->grid : num_tasks;
-    const size_t smem = (size_t)bins * bins / 2 * sizeof(uint32_t);
-    joint_histogram_mi_kernel<<<grid, HIST_THREADS, smem, st>>>(a);
+    const size_t smem = (size_t)packed_words(bins) * sizeof(uint32_t);
+    mi_kernel_for(bins)<<<grid, HIST_THREADS, smem, st>>>(a);
     ISO_CUDA(cudaGetLastError());
     int err = 0;
     ISO_CUDA(cudaMemcpyAsync(&err, ctrl + 1, sizeof(int), cudaMemcpyDeviceToHost, st));

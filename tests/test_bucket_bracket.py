@@ -1,19 +1,20 @@
-"""CPU check of the histogram kernels' fixed-point bucket arithmetic.
+"""CPU check of the histogram kernels' bracketed bucket arithmetic.
 
 The kernels bucket a value v of a pair with interval minimum mn and step
-step = RN((mx - mn) / bins) as s = RN(RN(v - mn) * RN(1/step) + 1536) (one
-fused multiply-add) and read the bucket from the bits of s; a value whose s
-is an exact integer (other than 0) is re-bucketed by IEEE division.  This test
-emulates that arithmetic bit for bit in integers (the exact product of the two
-float32 significands, one round-to-nearest-even onto the 2^-13 grid of s) and
-checks it against the reference's rule int(RN(RN(v - mn) / step)), clamped to
-[0, bins - 1], for every value the fast path keeps.
+step = RN((mx - mn) / bins) from d = RN(v - mn) and two widened reciprocals
+of r = RN(1/step): rlo = RD(r * (1 - 2^-22)) and rhi = RU(r * (1 + 2^-22)).
+Two packed fused multiply-adds give floor(d * rlo) and floor(d * rhi)
+exactly; where they agree that floor is the bucket, otherwise (and for NaN)
+the value is re-bucketed by IEEE division.  This test emulates that
+arithmetic bit for bit in integers (exact products of float32 significands)
+and checks it against the reference's rule int(RN(RN(v - mn) / step)),
+clamped to [0, bins - 1], for every value the fast path keeps.
 """
 import numpy as np
 import pytest
 
-BASE = np.float32(1536.0)
-BASE_BITS = 0x44C00000
+LO = 1.0 - 2.0 ** -22
+HI = 1.0 + 2.0 ** -22
 
 
 def reference_bucket(v, mn, step, bins):
@@ -32,41 +33,12 @@ def _significand(x):
     return m, e
 
 
-def fixed_point_bucket(v, mn, step, bins):
-    """Returns (bucket, ambiguous) as the kernels compute them."""
-    r = np.float32(1.0) / np.float32(step)           # RN(1/step)
-    d = (v - mn).astype(np.float32)                   # RN(v - mn), >= 0 here
+def exact_floor(d, r, bins):
+    """floor(d * r) of float32 d >= 0 and float32 r, exactly, clamped to bins - 1:
+    what RD(d * r + 2^23) - 2^23 gives in one fused multiply-add."""
     md, ed = _significand(d)
     mr, er = _significand(np.full_like(d, r))
     prod = md * mr                                    # < 2^48, exact
-    sh = ed + er + 13                                 # d*r*2^13 = prod * 2^sh
-    n = np.zeros_like(prod)
-    up = sh >= 0
-    n[up] = prod[up] << sh[up]
-    k = np.clip(-sh, 1, 62)
-    dn = (~up) & (-sh <= 62)
-    q = prod >> k
-    rem = prod & ((np.int64(1) << k) - 1)
-    half = np.int64(1) << (k - 1)
-    rnd = (rem > half) | ((rem == half) & ((q & 1) == 1))
-    n[dn] = (q + rnd)[dn]                             # round half to even
-    # s = 1536 + n * 2^-13 while n < 2^22 (q' < 512), so bits(s) = bits(1536) + n
-    assert n.max(initial=0) < (1 << 22)
-    u = BASE_BITS + n
-    kb = BASE_BITS >> 13
-    bucket = np.minimum(u >> 13, kb + bins - 1) - kb
-    ambiguous = ((u & 0x1FFF) == 0) & (u != BASE_BITS)
-    return bucket, ambiguous
-
-
-def floor_bucket(v, mn, step, bins):
-    """The kernels' bucket: RD(RN(v - mn) * RN(1/step) + 2^23) - 2^23 = the
-    floor of the exact product, clamped to bins - 1 (exact integer emulation)."""
-    r = np.float32(1.0) / np.float32(step)
-    d = (v - mn).astype(np.float32)
-    md, ed = _significand(d)
-    mr, er = _significand(np.full_like(d, r))
-    prod = md * mr
     sh = ed + er
     fl = np.zeros_like(prod)
     up = sh >= 0
@@ -75,6 +47,28 @@ def floor_bucket(v, mn, step, bins):
     dn = (~up) & (-sh <= 62)
     fl[dn] = (prod >> k)[dn]
     return np.minimum(fl, bins - 1)
+
+
+def widened_reciprocals(step):
+    """(RD(r * (1 - 2^-22)), RU(r * (1 + 2^-22))) with r = RN(1/step); both
+    products are exact in float64 and then rounded once to float32."""
+    r = np.float32(1.0) / np.float32(step)
+    lo64, hi64 = float(r) * LO, float(r) * HI
+    lo, hi = np.float32(lo64), np.float32(hi64)
+    if float(lo) > lo64:
+        lo = np.nextafter(lo, np.float32(-np.inf))
+    if float(hi) < hi64:
+        hi = np.nextafter(hi, np.float32(np.inf))
+    return lo, hi
+
+
+def bracket_bucket(v, mn, step, bins):
+    """Returns (bucket, ambiguous) as the kernels compute them."""
+    d = (v - mn).astype(np.float32)                   # RN(v - mn), >= 0 here
+    rlo, rhi = widened_reciprocals(step)
+    flo = exact_floor(d, rlo, bins + 2)
+    fhi = exact_floor(d, rhi, bins + 2)
+    return np.minimum(flo, bins - 1), flo != fhi
 
 
 def intervals(rng, count):
@@ -116,19 +110,49 @@ def test_fast_path_agrees_with_division(bins):
         ]).astype(np.float32)
         vals = vals[(vals >= mn) & (vals <= mx)]
         ref = reference_bucket(vals, mn, step, bins)
-        fx, amb = fixed_point_bucket(vals, mn, step, bins)
+        fx, amb = bracket_bucket(vals, mn, step, bins)
         ok = ~amb
         assert np.array_equal(fx[ok], ref[ok]), (mn, mx, bins)
-        # the bucket the kernels count (floor of the exact product) agrees too
-        assert np.array_equal(floor_bucket(vals, mn, step, bins)[ok], ref[ok]), (mn, mx, bins)
         kept += int(ok.sum())
         flagged += int(amb.sum())
         # v == mn (q = 0) stays on the fast path
-        f0, a0 = fixed_point_bucket(np.array([mn], np.float32), mn, step, bins)
+        f0, a0 = bracket_bucket(np.array([mn], np.float32), mn, step, bins)
         assert f0[0] == 0 and not a0[0]
     assert kept > 100000
-    # the exact division is rare: about 2^-13 of random values plus the edges
+    # the exact division is rare: about 2^-20 * q of random values plus edges
     assert flagged < 0.05 * kept
+
+
+def test_bracket_holds_at_every_quotient_boundary():
+    """Values whose quotient lies within a few ulps of every integer k, for
+    steps with awkward reciprocals: the floors bracket the reference's bucket
+    (floor(d * rlo) <= bucket <= floor(d * rhi)) for every one of them."""
+    rng = np.random.default_rng(11)
+    for _ in range(200):
+        bins = int(rng.choice([2, 7, 100, 224, 256]))
+        mn = np.float32(rng.uniform(-3, 3))
+        step = np.float32(10.0 ** rng.uniform(-6, 2))
+        mx = np.float32(mn + np.float32(bins) * step)
+        step = np.float32((mx - mn) / np.float32(bins))
+        if not (np.isfinite(step) and step > 0):
+            continue
+        k = np.arange(1, bins, dtype=np.float64)
+        v = (np.float64(mn) + k * np.float64(step)).astype(np.float32)
+        around = [v]
+        for _ in range(3):
+            around.append(np.nextafter(around[-1], np.float32(np.inf)))
+        w = v
+        for _ in range(3):
+            w = np.nextafter(w, np.float32(-np.inf))
+            around.append(w)
+        vals = np.concatenate(around)
+        vals = vals[(vals >= mn) & (vals <= mx)]
+        ref = reference_bucket(vals, mn, step, bins)
+        d = (vals - mn).astype(np.float32)
+        rlo, rhi = widened_reciprocals(step)
+        flo = exact_floor(d, rlo, 1 << 20)
+        fhi = exact_floor(d, rhi, 1 << 20)
+        assert np.all(np.minimum(flo, bins - 1) <= ref) and np.all(ref <= np.minimum(fhi, bins - 1))
 
 
 def test_every_value_stays_inside_the_histogram():
@@ -137,27 +161,15 @@ def test_every_value_stays_inside_the_histogram():
     mn, mx, bins = np.float32(0.25), np.float32(3.0), 256
     step = np.float32((mx - mn) / np.float32(bins))
     v = np.array([mx, np.nextafter(mx, np.float32(9)), mx * 1.001], np.float32)
-    fx, _ = fixed_point_bucket(v, mn, step, bins)
+    fx, _ = bracket_bucket(v, mn, step, bins)
     assert fx.min() >= 0 and fx.max() <= bins - 1
 
 
-def test_lowest_set_bit_form_of_the_ambiguity_test():
-    """The kernels test 'w is a nonzero multiple of 2^13' (u = bits(1536) | w)
-    as 'the lowest set bit of u lies in bits 13..21' so that eight values
-    combine with one OR; exhaustive over every u of the fixed-point range."""
-    u = (BASE_BITS + np.arange(1 << 22, dtype=np.int64)).astype(np.uint32)
-    direct = ((u & 0x1FFF) == 0) & (u != BASE_BITS)
-    low = u & (np.uint32(0) - u)
-    assert np.array_equal((low & np.uint32(0x3FE000)) != 0, direct)
-
-
-def test_multiply_high_forms():
-    """x >> 13 == umulhi(x, 2^19) and x >> 1 == umulhi(x, 2^31); the counted
-    half of a word wraps exactly when old * (65536 - odd * 65535) >= 0xFFFF0000."""
+def test_wrap_test_form():
+    """The counted half of a word wraps exactly when
+    old * (65536 - odd * 65535) >= 0xFFFF0000 (low 32 bits of the product)."""
     rng = np.random.default_rng(4)
     x = rng.integers(0, 1 << 32, 100000, dtype=np.uint64)
-    assert np.array_equal((x * (1 << 19)) >> 32, x >> 13)
-    assert np.array_equal((x * (1 << 31)) >> 32, x >> 1)
     old = np.concatenate([x, [0xFFFF, 0xFFFF0000, 0x1234FFFF, 0xFFFF1234, 0xFFFFFFFF, 0]]).astype(np.uint64)
     for odd in (0, 1):
         sh = 65536 - odd * 65535

@@ -252,7 +252,7 @@ def test_schedules_agree(ctx):
 def test_nan_values_take_bucket_zero(ctx):
     """NaN never enters a field interval (the comparisons in getInterval fail)
     and converts to bucket 0 in the reference's GPU kernel ((int)NaN is 0 on
-    the device); the fixed-point path hands NaN values to the division."""
+    the device); the fast path hands NaN values to the division."""
     f = fields_like_df(3, 100003, seed=5)
     f[0, ::997] = np.nan
     f[2, 5::1231] = np.nan
