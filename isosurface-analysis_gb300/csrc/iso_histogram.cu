@@ -102,11 +102,11 @@ __device__ __noinline__ int4 exact_bins4(float mn, float step, int bins, int rs,
 //   lo = RD(d * rlo + 2^23)   = 2^23 + floor(d * rlo)  (ulp 1 in [2^23, 2^24)),
 //   hi = RU(d * -rhi - 2^23)  = -(2^23 + floor(d * rhi)),
 // and lo + hi = floor(d * rlo) - floor(d * rhi) <= 0 is exact.  Where it is 0
-// the bucket is bits(lo) - bits(2^23).  The sum of lo + hi over the eight
-// values of four voxels is 0 exactly when every pair of floors agrees; a NaN
-// value makes it NaN.  Either way the four voxels take the division, which
-// happens for about 2^-20 * q of the values.  Near q = bins the bucket is
-// clamped to the last bin on both paths.
+// (+0.0, all bits clear) the bucket is bits(lo) - bits(2^23).  One OR over the
+// bits of the eight sums of four voxels is 0 exactly when every pair of floors
+// agrees; a NaN value gives a NaN sum, whose bits are not 0.  Otherwise the
+// four voxels take the division, which happens for about 2^-20 * q of the
+// values.  Near q = bins the bucket is clamped to the last bin on both paths.
 constexpr float FLOOR_BASE = 8388608.0f;  // 2^23
 constexpr uint32_t FLOOR_BASE_BITS = 0x4B000000u;
 
@@ -140,9 +140,8 @@ __device__ __forceinline__ void bins4(const Binner &bn, const float4 &x, const f
         const float2 ly01 = __ffma2_rd(dy01, rl, pb), ly23 = __ffma2_rd(dy23, rl, pb);
         const float2 hx01 = __ffma2_ru(dx01, nrh, nb), hx23 = __ffma2_ru(dx23, nrh, nb);
         const float2 hy01 = __ffma2_ru(dy01, nrh, nb), hy23 = __ffma2_ru(dy23, nrh, nb);
-        const float2 zx = __fadd2_rn(__fadd2_rn(lx01, hx01), __fadd2_rn(lx23, hx23));
-        const float2 zy = __fadd2_rn(__fadd2_rn(ly01, hy01), __fadd2_rn(ly23, hy23));
-        const float2 z = __fadd2_rn(zx, zy);
+        const float2 zx01 = __fadd2_rn(lx01, hx01), zx23 = __fadd2_rn(lx23, hx23);
+        const float2 zy01 = __fadd2_rn(ly01, hy01), zy23 = __fadd2_rn(ly23, hy23);
         // bucket = min(bits(lo) - bits(2^23), bins - 1) as unsigned: any input
         // (also one outside the interval) stays inside the histogram
         const uint32_t top = (uint32_t)(bins - 1);
@@ -155,7 +154,9 @@ __device__ __forceinline__ void bins4(const Binner &bn, const float4 &x, const f
                    min(__float_as_uint(ly23.x) - FLOOR_BASE_BITS, top));
         b3 = (int)(min(__float_as_uint(lx23.y) - FLOOR_BASE_BITS, top) * ub +
                    min(__float_as_uint(ly23.y) - FLOOR_BASE_BITS, top));
-        const bool slow = !(__fadd_rn(z.x, z.y) == 0.0f);
+        const bool slow = ((__float_as_uint(zx01.x) | __float_as_uint(zx01.y) | __float_as_uint(zx23.x) |
+                            __float_as_uint(zx23.y) | __float_as_uint(zy01.x) | __float_as_uint(zy01.y) |
+                            __float_as_uint(zy23.x) | __float_as_uint(zy23.y)) != 0u);
         if (__builtin_expect(slow, 0)) {
             const int4 e = RELOAD ? exact_bins4_at(bn.mn, bn.step, bins, rstride, p1, p2, q)
                                   : exact_bins4(bn.mn, bn.step, bins, rstride, x, y);
@@ -199,20 +200,22 @@ __device__ __noinline__ void log_wrap(int bin, uint32_t sh, uint32_t old, int4 *
 }
 
 // Counts four bins.  A bin is a 16-bit half of word bin/2 (odd bins in the
-// high half).  old * (odd ? 1 : 65536) moves the counted half of the old word
-// to the top 16 bits, so the half wrapped exactly when that product is
-// >= 0xFFFF0000; one test covers the four updates, and the rare wraps go to
-// wrap(bin, odd, old).
+// high half); its increment is 1 or 65536.  old * (increment ^ 0x10001), i.e.
+// old * 65536 for the low half and old * 1 for the high half, moves the
+// counted half of the old word to the top 16 bits, so the half wrapped exactly
+// when that product is >= 0xFFFF0000; one test covers the four updates, and
+// the rare wraps go to wrap(bin, odd, old).
 template <class Wrap>
 __device__ __forceinline__ void count4(uint32_t *words, int b0, int b1, int b2, int b3, const Wrap &wrap)
 {
     const uint32_t o0 = (uint32_t)b0 & 1u, o1 = (uint32_t)b1 & 1u, o2 = (uint32_t)b2 & 1u, o3 = (uint32_t)b3 & 1u;
-    const uint32_t old0 = atomicAdd(&words[b0 >> 1], o0 * 0xFFFFu + 1u);
-    const uint32_t old1 = atomicAdd(&words[b1 >> 1], o1 * 0xFFFFu + 1u);
-    const uint32_t old2 = atomicAdd(&words[b2 >> 1], o2 * 0xFFFFu + 1u);
-    const uint32_t old3 = atomicAdd(&words[b3 >> 1], o3 * 0xFFFFu + 1u);
-    const uint32_t t0 = old0 * (65536u - o0 * 65535u), t1 = old1 * (65536u - o1 * 65535u);
-    const uint32_t t2 = old2 * (65536u - o2 * 65535u), t3 = old3 * (65536u - o3 * 65535u);
+    const uint32_t i0 = o0 * 0xFFFFu + 1u, i1 = o1 * 0xFFFFu + 1u, i2 = o2 * 0xFFFFu + 1u, i3 = o3 * 0xFFFFu + 1u;
+    const uint32_t old0 = atomicAdd(&words[b0 >> 1], i0);
+    const uint32_t old1 = atomicAdd(&words[b1 >> 1], i1);
+    const uint32_t old2 = atomicAdd(&words[b2 >> 1], i2);
+    const uint32_t old3 = atomicAdd(&words[b3 >> 1], i3);
+    const uint32_t t0 = old0 * (i0 ^ 0x10001u), t1 = old1 * (i1 ^ 0x10001u);
+    const uint32_t t2 = old2 * (i2 ^ 0x10001u), t3 = old3 * (i3 ^ 0x10001u);
     if (__builtin_expect(max(max(t0, t1), max(t2, t3)) >= 0xFFFF0000u, 0)) {
         if (t0 >= 0xFFFF0000u) wrap(b0, o0, old0);
         if (t1 >= 0xFFFF0000u) wrap(b1, o1, old1);

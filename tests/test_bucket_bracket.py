@@ -166,13 +166,16 @@ def test_every_value_stays_inside_the_histogram():
 
 
 def test_wrap_test_form():
-    """The counted half of a word wraps exactly when
-    old * (65536 - odd * 65535) >= 0xFFFF0000 (low 32 bits of the product)."""
+    """The counted half of a word wraps exactly when old * (inc ^ 0x10001)
+    >= 0xFFFF0000 (low 32 bits of the product), inc = odd * 0xFFFF + 1 being
+    the half's increment (1 or 65536)."""
     rng = np.random.default_rng(4)
     x = rng.integers(0, 1 << 32, 100000, dtype=np.uint64)
     old = np.concatenate([x, [0xFFFF, 0xFFFF0000, 0x1234FFFF, 0xFFFF1234, 0xFFFFFFFF, 0]]).astype(np.uint64)
     for odd in (0, 1):
-        sh = 65536 - odd * 65535
+        inc = odd * 0xFFFF + 1
+        sh = inc ^ 0x10001
+        assert sh == 65536 - odd * 65535
         t = (old * sh) & 0xFFFFFFFF
         half = (old >> (16 * odd)) & 0xFFFF
         assert np.array_equal(t >= 0xFFFF0000, half == 0xFFFF)
