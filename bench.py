@@ -494,7 +494,7 @@ def run_multi(args):
     F = S ** 3
     stride = (F + 63) // 64 * 64
     ctx = isosim.Context(local)
-    stats = {"ism_pairs": 0, "t_ism": 0.0}
+    stats = {"ism_pairs": 0, "t_ism": 0.0, "stage_ms": np.zeros(3)}
 
     # this rank's volumes are generated before the timed batch (the engine's
     # input, like a volume loaded from disk)
@@ -510,8 +510,9 @@ def run_multi(args):
             t0 = time.perf_counter()
             vmin, vmax = float(vol.min()), float(vol.max())
             isos = np.array([vmin + (i + 1) * (vmax - vmin) / (n + 1) for i in range(n)], np.float32)
-            ism, ids, _, _ = ctx.ism(vol, shape, isos, bins=bins)
+            ism, ids, _, timing = ctx.ism(vol, shape, isos, bins=bins)
             stats["ism_pairs"] += len(ids) * (len(ids) - 1) // 2
+            stats["stage_ms"] += [timing.surface_ms, timing.distance_ms, timing.histogram_ms]
             picks = sorted(r[3] for r in isosim.select_representatives(ism, ids, isos, reps))
             for q, row in enumerate(picks):
                 ctx.copy_field(row, rows[(vid - lo) * reps + q])
@@ -555,7 +556,10 @@ def run_multi(args):
                            "parallelism": "volumes sharded over %d rank(s); one all-gather of representative "
                                           "fields" % world},
                 "wall_s": round(wall, 3),
-                "rank0_ism_stage": {"pairs": int(stats["ism_pairs"]), "seconds": round(stats["t_ism"], 3)},
+                "rank0_ism_stage": {"pairs": int(stats["ism_pairs"]), "seconds": round(stats["t_ism"], 3),
+                                    "engine_stage_s": {k: round(float(v) / 1e3, 3) for k, v in
+                                                       zip(("surfaces", "distance_fields", "histograms_nmi"),
+                                                           stats["stage_ms"])}},
                 "rank0_cross_stage": {"pairs": int(stats.get("cross_pairs", 0)),
                                       "seconds": round(stats.get("t_cross", 0.0), 3)},
                 "tsm_vsm_sample": {"first_blocks": [[int(a), int(b), round(float(x), 4), round(float(y), 4)]
