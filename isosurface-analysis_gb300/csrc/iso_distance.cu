@@ -330,6 +330,10 @@ constexpr int PATCH_Z = 8, PATCH_Y = 4, WARPS_Y = QUERY_THREADS / 32;
 // short runs keep enough blocks in flight for small volumes
 constexpr int RUN_X_LONG = 64, RUN_X_SHORT = 8;
 constexpr int QUERY_GROUP = 4;  // samples per lane traversed together
+// neighbour lanes whose last nearest point is a further candidate bound:
+// z +- 1, y +- 1 and z +- 2 (lane xor 1, xor 8, xor 2; 256^3 distance stage
+// 291 ms with the first two, 287 ms with three, 289 ms adding y +- 2)
+constexpr int NEIGHBOURS = 3;
 
 __device__ __forceinline__ void load_node(const BvhNode *nodes, int cur, float4 &a, float4 &b, float4 &c, int4 &d)
 {
@@ -493,14 +497,15 @@ __global__ void __launch_bounds__(QUERY_THREADS, 8) bvh_query_kernel(Bvh b, Samp
     for (int k0 = 0; k0 < RUN_X; k0 += K) {
         if (!__any_sync(0xffffffffu, col_valid && x0 + k0 < X10)) break;
         // candidates (all real points, so every bound is a true distance):
-        // the previous group's last two nearest points and the z and y
-        // neighbour lanes' last one (for the first group, the greedy points)
-        float3 cand[4];
+        // the previous group's last two nearest points and the last one of
+        // the neighbour lanes z +- 1, y +- 1, z +- 2 (for the first group, the
+        // greedy points)
+        float3 cand[2 + NEIGHBOURS];
         cand[0] = p_last;
         cand[1] = p_prev;
 #pragma unroll
-        for (int o = 0; o < 2; ++o) {
-            const int mask = o == 0 ? 1 : PATCH_Z;
+        for (int o = 0; o < NEIGHBOURS; ++o) {
+            const int mask = o == 0 ? 1 : (o == 1 ? PATCH_Z : (o == 2 ? 2 : 2 * PATCH_Z));
             cand[2 + o].x = __shfl_xor_sync(0xffffffffu, p_last.x, mask);
             cand[2 + o].y = __shfl_xor_sync(0xffffffffu, p_last.y, mask);
             cand[2 + o].z = __shfl_xor_sync(0xffffffffu, p_last.z, mask);
@@ -525,7 +530,7 @@ __global__ void __launch_bounds__(QUERY_THREADS, 8) bvh_query_kernel(Bvh b, Samp
                 pts[k] = bp;
             }
 #pragma unroll
-            for (int o = 1; o < 4; ++o) {
+            for (int o = 1; o < 2 + NEIGHBOURS; ++o) {
                 const float cd = iso_dist2(__fsub_rn(sk.x, cand[o].x), __fsub_rn(sk.y, cand[o].y),
                                            __fsub_rn(sk.z, cand[o].z));
                 if (cd < bst[k]) {
