@@ -152,7 +152,6 @@ struct Bvh {
     float4 *leaves;          // sorted points
     BvhNode *nodes;          // segment s owns nodes [cstart[s]-s, cstart[s]-s+count-1)
     int *parent_node;        // per internal node: parent*2 + side, -1 at the root
-    int *parent_leaf;        // per leaf: parent*2 + side, -1 for a one-leaf segment
     unsigned int *flags;
     int *error;
 };
@@ -184,6 +183,20 @@ __device__ __forceinline__ int karras_delta(const unsigned long long *codes, int
     return __clz(ci ^ cj);
 }
 
+__device__ __forceinline__ void store_box(BvhNode *node, int side, float3 lo, float3 hi)
+{
+    float *a = &node->a.x, *b = &node->b.x, *c = &node->c.x;
+    __stcg(a + side, lo.x);
+    __stcg(a + 2 + side, lo.y);
+    __stcg(b + side, lo.z);
+    __stcg(b + 2 + side, -hi.x);
+    __stcg(c + side, -hi.y);
+    __stcg(c + 2 + side, -hi.z);
+}
+
+// One thread per internal node (Karras split).  Leaf children's boxes (their
+// points) are written here, and each node's arrival flag starts at its number
+// of leaf children, so the box pass starts at the nodes with two leaves.
 __global__ void bvh_build_kernel(Bvh b, const unsigned long long *sorted_keys)
 {
     int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -225,23 +238,25 @@ __global__ void bvh_build_kernel(Bvh b, const unsigned long long *sorted_keys)
     const int right = (last == split + 1) ? ((split + 1) | LEAF_BIT) : split + 1;
 
     BvhNode *node = b.nodes + nbase + i;
+    const bool ll = (left & LEAF_BIT) != 0, rl = (right & LEAF_BIT) != 0;
+    const float4 *lv = b.leaves + b.cstart[s];
+    if (ll && rl) {
+        const float4 p = lv[left & ~LEAF_BIT], q = lv[right & ~LEAF_BIT];
+        node->a = make_float4(p.x, q.x, p.y, q.y);
+        node->b = make_float4(p.z, q.z, -p.x, -q.x);
+        node->c = make_float4(-p.y, -q.y, -p.z, -q.z);
+    } else if (ll) {
+        const float4 p = lv[left & ~LEAF_BIT];
+        store_box(node, 0, make_float3(p.x, p.y, p.z), make_float3(p.x, p.y, p.z));
+    } else if (rl) {
+        const float4 q = lv[right & ~LEAF_BIT];
+        store_box(node, 1, make_float3(q.x, q.y, q.z), make_float3(q.x, q.y, q.z));
+    }
     node->d = make_int4(left, right, 0, 0);
-    if (left & LEAF_BIT) b.parent_leaf[b.cstart[s] + (left & ~LEAF_BIT)] = i * 2 + 0;
-    else b.parent_node[nbase + left] = i * 2 + 0;
-    if (right & LEAF_BIT) b.parent_leaf[b.cstart[s] + (right & ~LEAF_BIT)] = i * 2 + 1;
-    else b.parent_node[nbase + right] = i * 2 + 1;
+    b.flags[nbase + i] = (unsigned int)ll + (unsigned int)rl;
+    if (!ll) b.parent_node[nbase + left] = i * 2 + 0;
+    if (!rl) b.parent_node[nbase + right] = i * 2 + 1;
     if (i == 0) b.parent_node[nbase] = -1;
-}
-
-__device__ __forceinline__ void store_box(BvhNode *node, int side, float3 lo, float3 hi)
-{
-    float *a = &node->a.x, *b = &node->b.x, *c = &node->c.x;
-    __stcg(a + side, lo.x);
-    __stcg(a + 2 + side, lo.y);
-    __stcg(b + side, lo.z);
-    __stcg(b + 2 + side, -hi.x);
-    __stcg(c + side, -hi.y);
-    __stcg(c + 2 + side, -hi.z);
 }
 
 // Arrival count with release (this thread's box stores before it) and
@@ -254,17 +269,26 @@ __device__ __forceinline__ unsigned int arrive_acq_rel(unsigned int *p)
     return old;
 }
 
+// Bottom-up boxes, one thread per internal node with two leaf children (its
+// box is complete after bvh_build_kernel).  A thread stores its node's box
+// into the parent and arrives there; the parent's flag counts leaf children
+// plus arrivals, so the thread that brings it to 2 carries on upwards.
 __global__ void bvh_boxes_kernel(Bvh b)
 {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.total) return;
-    int s = find_segment(b.cstart, b.m, i);
-    // a segment with one leaf has no internal node
-    if (b.ccount[s] < 2) return;
-    const int64_t nbase = b.cstart[s] - s;
-    float4 p = b.leaves[i];
-    float3 lo = make_float3(p.x, p.y, p.z), hi = lo;
-    int link = b.parent_leaf[i];
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= b.total - b.m) return;
+    const int4 cd = b.nodes[g].d;
+    if (!((cd.x & LEAF_BIT) && (cd.y & LEAF_BIT))) return;
+    int lo_s = 0, hi_s = b.m - 1;  // the segment owning node g (as in bvh_build_kernel)
+    while (lo_s < hi_s) {
+        const int mid = (lo_s + hi_s + 1) >> 1;
+        if (b.cstart[mid] - mid <= g) lo_s = mid; else hi_s = mid - 1;
+    }
+    const int64_t nbase = b.cstart[lo_s] - lo_s;
+    const float4 ga = __ldcg(&b.nodes[g].a), gb = __ldcg(&b.nodes[g].b), gc = __ldcg(&b.nodes[g].c);
+    float3 lo = make_float3(fminf(ga.x, ga.y), fminf(ga.z, ga.w), fminf(gb.x, gb.y));
+    float3 hi = make_float3(-fminf(gb.z, gb.w), -fminf(gc.x, gc.y), -fminf(gc.z, gc.w));
+    int link = b.parent_node[g];
     // depth is bounded by the 62-bit augmented key, the loop by the node count
     for (int guard = 0; guard < 4096 && link >= 0; ++guard) {
         const int parent = link >> 1, side = link & 1;
@@ -562,7 +586,7 @@ static int lbvh_group(iso_ctx *ctx, const SampleGrid &g, Segments sg, const int6
         total += h_count[q];
     }
     if (total >= (int64_t)0x7fffffff) return iso_fail(ISO_ERR_CAPACITY, "too many surface points (%lld)", (long long)total);
-    void *d_cstart, *d_keys, *d_keys2, *d_vals, *d_vals2, *d_compact, *d_leaves, *d_nodes, *d_pn, *d_pl, *d_flags, *d_misc;
+    void *d_cstart, *d_keys, *d_keys2, *d_vals, *d_vals2, *d_compact, *d_leaves, *d_nodes, *d_pn, *d_flags, *d_misc;
     ISO_TRY(iso_buf(ctx, BUF_STAGING_A, (size_t)m * 2 * sizeof(int64_t), &d_cstart));
     ISO_TRY(iso_buf(ctx, BUF_SORT_KEYS, (size_t)total * 8, &d_keys));
     ISO_TRY(iso_buf(ctx, BUF_SORT_KEYS_ALT, (size_t)total * 8, &d_keys2));
@@ -571,17 +595,15 @@ static int lbvh_group(iso_ctx *ctx, const SampleGrid &g, Segments sg, const int6
     ISO_TRY(iso_buf(ctx, BUF_STAGING_B, (size_t)total * sizeof(float4), &d_compact));
     ISO_TRY(iso_buf(ctx, BUF_BVH_LEAVES, (size_t)total * sizeof(float4), &d_leaves));
     ISO_TRY(iso_buf(ctx, BUF_BVH_NODES, (size_t)total * sizeof(BvhNode), &d_nodes));
-    ISO_TRY(iso_buf(ctx, BUF_BVH_PARENT, (size_t)total * 2 * sizeof(int), &d_pn));
+    ISO_TRY(iso_buf(ctx, BUF_BVH_PARENT, (size_t)total * sizeof(int), &d_pn));
     ISO_TRY(iso_buf(ctx, BUF_BVH_FLAGS, (size_t)total * sizeof(unsigned int), &d_flags));
     ISO_TRY(iso_buf(ctx, BUF_MISC, 256, &d_misc));
-    d_pl = (int *)d_pn + total;
     std::vector<int64_t> cs2(2 * (size_t)m);
     for (int q = 0; q < m; ++q) {
         cs2[q] = cstart[q];
         cs2[m + q] = h_count[q];
     }
     ISO_CUDA(cudaMemcpyAsync(d_cstart, cs2.data(), cs2.size() * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
-    ISO_CUDA(cudaMemsetAsync(d_flags, 0, (size_t)total * sizeof(unsigned int), ctx->stream));
     ISO_CUDA(cudaMemsetAsync(d_misc, 0, sizeof(int), ctx->stream));
     Segments gs = sg;  // segment offsets of this group
     gs.offset = sg.offset + seg0;
@@ -597,7 +619,6 @@ static int lbvh_group(iso_ctx *ctx, const SampleGrid &g, Segments sg, const int6
     b.leaves = (float4 *)d_leaves;
     b.nodes = (BvhNode *)d_nodes;
     b.parent_node = (int *)d_pn;
-    b.parent_leaf = (int *)d_pl;
     b.flags = (unsigned int *)d_flags;
     b.error = (int *)d_misc;
     const unsigned tb = (unsigned)((total + 255) / 256);
@@ -619,7 +640,7 @@ static int lbvh_group(iso_ctx *ctx, const SampleGrid &g, Segments sg, const int6
     if (total_nodes > 0) {
         bvh_build_kernel<<<(unsigned)((total_nodes + 255) / 256), 256, 0, ctx->stream>>>(b, kb.Current());
         ISO_LAUNCHED(ctx);
-        bvh_boxes_kernel<<<tb, 256, 0, ctx->stream>>>(b);
+        bvh_boxes_kernel<<<(unsigned)((total_nodes + 255) / 256), 256, 0, ctx->stream>>>(b);
         ISO_LAUNCHED(ctx);
     }
     for (int base = 0; base < m; base += 65535) {
