@@ -114,6 +114,10 @@ ISO_API int64_t iso_ctx_launches(iso_ctx *ctx);
                                             slice of their fields; up to 1 GB of per-pair histograms);
                                             0 = never; otherwise a multiple of 4, at least 65536;
                                             default 2097152 */
+#define ISO_LIMIT_SURF_BLOCK_COUNT_BYTES 3 /* marching cubes keeps each block's vertex counts between
+                                               its count and write passes while that table takes at
+                                               most this many bytes (default 2^30), else the write
+                                               pass counts again; 0 = always count again */
 ISO_API int iso_ctx_set_limit(iso_ctx *ctx, int which, int64_t value);
 
 /* ---------------------------------------------------------------------- */

@@ -75,7 +75,7 @@ void iso_ctx_release_except_surfaces(iso_ctx *ctx)
     cudaStreamSynchronize(ctx->stream);
     for (int b = 0; b < BUF_COUNT_; ++b) {
         if (b == BUF_VOLUME || b == BUF_ISO_SORTED || b == BUF_SURF_COUNTS || b == BUF_SURF_CURSOR ||
-            b == BUF_SEG_OFFSET || b == BUF_SEG_COUNT)
+            b == BUF_SEG_OFFSET || b == BUF_SEG_COUNT || b == BUF_SURF_BLOCK_COUNTS)
             continue;
         if (ctx->buf[b]) cudaFree(ctx->buf[b]);
         ctx->buf[b] = nullptr;
@@ -97,6 +97,10 @@ extern "C" int iso_ctx_set_limit(iso_ctx *ctx, int which, int64_t value)
         if (value != 0 && (value < 65536 || value % 4 != 0))
             return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: segment length must be 0 or a multiple of 4 >= 65536");
         ctx->hist_segment_values = value;
+        return ISO_OK;
+    case ISO_LIMIT_SURF_BLOCK_COUNT_BYTES:
+        if (value < 0) return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: byte limit must be >= 0");
+        ctx->surf_block_count_bytes = value;
         return ISO_OK;
     default:
         return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: unknown limit %d", which);

@@ -42,12 +42,15 @@ void iso_clear_error();
     } while (0)
 
 constexpr int ISO_MAX_BINS = 256;
-// LBVH surfaces are built and queried in groups of at most this many points
-// (default of iso_ctx_set_limit(ISO_LIMIT_LBVH_GROUP_POINTS))
 constexpr int64_t ISO_HIST_SEGMENT_VALUES = 2097152;  // segment-major above 2^21 values (226..256 bins)
 constexpr int ISO_WIDE_MAX_BINS = 224;                // up to this many bins: 32-bit counters, one CTA per pair
 constexpr size_t ISO_HIST_CHUNK_BYTES = (size_t)1 << 30;  // per-pair global histograms of one segment-major chunk
+// LBVH surfaces are built and queried in groups of at most this many points
+// (default of iso_ctx_set_limit(ISO_LIMIT_LBVH_GROUP_POINTS))
 constexpr int64_t ISO_LBVH_GROUP_POINTS = (int64_t)1 << 27;
+// marching cubes: default of the largest per-block count table kept between
+// the count and write passes (256 isovalues of a 256^3 volume take 136 MB)
+constexpr int64_t ISO_SURF_BLOCK_COUNT_BYTES = (int64_t)1 << 30;
 
 // ---------------------------------------------------------------------------
 // device arena: named grow-only buffers owned by a context
@@ -85,6 +88,7 @@ enum IsoBuf {
     BUF_STAGING_B,
     BUF_CLNC,            // c*ln(c) for c < 65536, FP64
     BUF_HIST_DUMP_SEG,   // per-pair global histograms of the segment-major schedule
+    BUF_SURF_BLOCK_COUNTS,  // marching cubes: per block and isovalue, the vertex versions it counted
     BUF_COUNT_
 };
 
@@ -105,6 +109,7 @@ struct iso_ctx {
     // request's device-memory need; a non-zero return aborts the request
     int64_t lbvh_group_points = ISO_LBVH_GROUP_POINTS;  // see iso_ctx_set_limit
     int64_t hist_segment_values = ISO_HIST_SEGMENT_VALUES;  // 0: one CTA per pair for every length
+    int64_t surf_block_count_bytes = ISO_SURF_BLOCK_COUNT_BYTES;  // see iso_ctx_set_limit
     int (*admit)(void *user, size_t bytes) = nullptr;
     void *admit_user = nullptr;
     // request shape for the admission estimate (set by iso_ism)
@@ -115,7 +120,8 @@ struct iso_ctx {
 // Frees every arena buffer of a context (the context stays usable).
 void iso_ctx_release(iso_ctx *ctx);
 // Frees every buffer except the ones a request holds between its surface count
-// pass and its admission (staged volume, sorted isovalues, counts, offsets).
+// pass and its admission (staged volume, sorted isovalues, counts, offsets, the
+// marching-cubes per-block counts that the write pass reads).
 void iso_ctx_release_except_surfaces(iso_ctx *ctx);
 
 // Ensures buffer `b` holds at least `bytes`; contents are not preserved.

@@ -148,6 +148,7 @@ struct SurfOut {
     float4 *points;
     unsigned long long *corner_keys;
     int64_t corner_stride;        // (gA+1)(gB+1)(gC+1)
+    unsigned int *block_counts;   // marching cubes: per block and k, [2] regular / corner versions counted
 };
 
 // Emits one vertex version.  phase 0: count; phase 1: write.
@@ -172,10 +173,12 @@ __device__ __forceinline__ void put_vertex(int phase, int k, float x, float y, f
     }
 }
 
-template <int PHASE>
+// PHASE 0: count vertex versions; PHASE 1: write them.  CLASSIFY: also count
+// the cell's active isovalues and triangle vertices (the count launch only).
+template <int PHASE, bool CLASSIFY>
 __device__ void mc_point(const Grid &g, int a, int b, int c, const float *s_iso, int n, unsigned int *s_reg,
                          unsigned int *s_cor, const unsigned long long *s_base, const SurfOut &o,
-                         unsigned long long *s_active, unsigned long long *s_total)
+                         unsigned int *s_active, unsigned int *s_total)
 {
     const float f0 = sample(g, a, b, c);
     // ---- x edge (a,b,c)-(a+1,b,c): forward users e0/e4, reverse users e2/e6
@@ -238,7 +241,7 @@ __device__ void mc_point(const Grid &g, int a, int b, int c, const float *s_iso,
         }
     }
     // ---- case codes of cell (a,b,c) for every isovalue in (min, max]
-    if (PHASE == 0 && cell_valid(g, a, b, c)) {
+    if (CLASSIFY && cell_valid(g, a, b, c)) {
         float f[8];
         f[0] = f0;
         f[1] = sample(g, a + 1, b, c);
@@ -263,8 +266,8 @@ __device__ void mc_point(const Grid &g, int a, int b, int c, const float *s_iso,
                 for (int q = 0; q < 8; ++q) cube |= (unsigned)(f[q] < iso) << q;
                 unsigned nv = c_mc_verts[cube];
                 if (nv) {
-                    atomicAdd(&s_active[k], 1ull);
-                    atomicAdd(&s_total[k], (unsigned long long)nv);
+                    atomicAdd(&s_active[k], 1u);
+                    atomicAdd(&s_total[k], nv);
                 }
             }
         }
@@ -287,16 +290,19 @@ __device__ __forceinline__ void point_of(const Grid &g, int64_t id, int &a, int 
     }
 }
 
-// mode 0: accumulate per-isovalue counts; mode 1: write vertices.
+// mode 0: accumulate per-isovalue counts and keep the block's own counts;
+// mode 1: reserve the block's slots from those counts and write vertices.
 __global__ void __launch_bounds__(SURF_THREADS) mc_kernel(Grid g, const float *iso_sorted, int n, SurfOut o, int mode)
 {
     extern __shared__ unsigned char smem_raw[];
     float *s_iso = reinterpret_cast<float *>(smem_raw);
     unsigned long long *s_base = reinterpret_cast<unsigned long long *>(s_iso + ((n + 1) & ~1));
-    unsigned long long *s_active = s_base + 2 * n;
-    unsigned long long *s_total = s_active + n;
-    unsigned int *s_reg = reinterpret_cast<unsigned int *>(s_total + n);
+    // per-block counts fit 32 bits (at most 15 triangle vertices per cell):
+    // native shared-memory atomics, widened when added to the global counts
+    unsigned int *s_reg = reinterpret_cast<unsigned int *>(s_base + 2 * n);
     unsigned int *s_cor = s_reg + n;
+    unsigned int *s_active = s_cor + n;
+    unsigned int *s_total = s_active + n;
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
         s_iso[k] = iso_sorted[k];
         s_reg[k] = 0;
@@ -310,25 +316,32 @@ __global__ void __launch_bounds__(SURF_THREADS) mc_kernel(Grid g, const float *i
     int a = 0, b = 0, c = 0;
     const bool live = id < total;
     if (live) point_of(g, id, a, b, c);
-    if (live) mc_point<0>(g, a, b, c, s_iso, n, s_reg, s_cor, s_base, o, s_active, s_total);
-    __syncthreads();
+    uint2 *own = o.block_counts ? reinterpret_cast<uint2 *>(o.block_counts) + (size_t)blockIdx.x * n : nullptr;
     if (mode == 0) {
+        if (live) mc_point<0, true>(g, a, b, c, s_iso, n, s_reg, s_cor, s_base, o, s_active, s_total);
+        __syncthreads();
         for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            if (own) own[k] = make_uint2(s_reg[k], s_cor[k]);
             if (s_reg[k]) atomicAdd(&o.counts[4 * k + 0], (unsigned long long)s_reg[k]);
             if (s_cor[k]) atomicAdd(&o.counts[4 * k + 1], (unsigned long long)s_cor[k]);
-            if (s_active[k]) atomicAdd(&o.counts[4 * k + 2], s_active[k]);
-            if (s_total[k]) atomicAdd(&o.counts[4 * k + 3], s_total[k]);
+            if (s_active[k]) atomicAdd(&o.counts[4 * k + 2], (unsigned long long)s_active[k]);
+            if (s_total[k]) atomicAdd(&o.counts[4 * k + 3], (unsigned long long)s_total[k]);
         }
         return;
     }
+    if (!own) {  // no room was kept for the block counts: count again
+        if (live) mc_point<0, false>(g, a, b, c, s_iso, n, s_reg, s_cor, s_base, o, s_active, s_total);
+        __syncthreads();
+    }
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        s_base[2 * k] = s_reg[k] ? atomicAdd(&o.cursor[2 * k], (unsigned long long)s_reg[k]) : 0;
-        s_base[2 * k + 1] = s_cor[k] ? atomicAdd(&o.cursor[2 * k + 1], (unsigned long long)s_cor[k]) : 0;
+        const uint2 cnt = own ? own[k] : make_uint2(s_reg[k], s_cor[k]);
+        s_base[2 * k] = cnt.x ? atomicAdd(&o.cursor[2 * k], (unsigned long long)cnt.x) : 0;
+        s_base[2 * k + 1] = cnt.y ? atomicAdd(&o.cursor[2 * k + 1], (unsigned long long)cnt.y) : 0;
         s_reg[k] = 0;
         s_cor[k] = 0;
     }
     __syncthreads();
-    if (live) mc_point<1>(g, a, b, c, s_iso, n, s_reg, s_cor, s_base, o, s_active, s_total);
+    if (live) mc_point<1, false>(g, a, b, c, s_iso, n, s_reg, s_cor, s_base, o, s_active, s_total);
 }
 
 // Voxel approximation, host frame, scale 1.
@@ -500,14 +513,23 @@ int iso_run_surfaces(iso_ctx *ctx, const float *d_vol, int X, int Y, int Z, cons
     o.points = nullptr;
     o.corner_keys = nullptr;
     o.corner_stride = (int64_t)(X + 1) * (Y + 1) * (Z + 1);
+    o.block_counts = nullptr;
 
     const bool mc = surface == ISO_SURFACE_MC;
     const size_t iso_bytes = (size_t)((n + 1) & ~1) * sizeof(float);
-    const size_t smem = mc ? iso_bytes + (size_t)n * (4 * sizeof(unsigned long long) + 2 * sizeof(unsigned int))
+    const size_t smem = mc ? iso_bytes + (size_t)n * (2 * sizeof(unsigned long long) + 4 * sizeof(unsigned int))
                            : iso_bytes + (size_t)n * (2 * sizeof(unsigned long long) + sizeof(unsigned int));
     const int64_t items = mc ? (int64_t)(X + 1) * (Y + 1) * (Z + 1) : (int64_t)(X - 1) * (Y - 1) * (Z - 1);
     const int64_t blocks = (items + SURF_THREADS - 1) / SURF_THREADS;
     if (blocks > 0x7fffffffLL) return iso_fail(ISO_ERR_ARG, "volume too large");
+    // marching cubes keeps each block's counts for the write pass (which then
+    // does not count again) while they fit the context's limit
+    const size_t bc_bytes = (size_t)blocks * n * 2 * sizeof(unsigned int);
+    if (mc && (int64_t)bc_bytes <= ctx->surf_block_count_bytes) {
+        void *d_bc;
+        ISO_TRY(iso_buf(ctx, BUF_SURF_BLOCK_COUNTS, bc_bytes, &d_bc));
+        o.block_counts = (unsigned int *)d_bc;
+    }
     if (smem > 48 * 1024) {
         ISO_CUDA(cudaFuncSetAttribute(mc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         ISO_CUDA(cudaFuncSetAttribute(approx_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -539,6 +561,7 @@ int iso_run_surfaces(iso_ctx *ctx, const float *d_vol, int X, int Y, int Z, cons
         // temporaries), distance fields, histogram scratch and the map
         const double P = (double)tot_pts, m = (double)nonempty;
         double need = 4.0 * ctx->plan_V * ctx->plan_volume_copy + 32.0 * P + 16.0 * tot_cor +
+                      (o.block_counts ? (double)bc_bytes : 0.0) +
                       (ctx->plan_lbvh ? 180.0 * std::min(P, (double)ctx->lbvh_group_points) : 0.0) +
                       4.0 * m * ctx->plan_stride + 12.0 * m * m +
                       8.0 * 65536 + 16.0 * (1 << 20);

@@ -183,6 +183,11 @@ class Context:
         """Fields longer than `values` use the segment-major histogram schedule (0: never)."""
         _check(lib.iso_ctx_set_limit(self.handle, 2, int(values)))
 
+    def set_surf_block_count_bytes(self, nbytes):
+        """Largest per-block vertex-count table marching cubes keeps between its
+        passes (0: the write pass counts again)."""
+        _check(lib.iso_ctx_set_limit(self.handle, 3, int(nbytes)))
+
     @property
     def launches(self):
         return int(lib.iso_ctx_launches(self.handle))

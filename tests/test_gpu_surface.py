@@ -40,6 +40,22 @@ def test_mc_noncubic_noise(ctx, frame):
     check_mc(ctx, vol, dims, np.array([-0.7, 0.0, 0.2, 1.1], np.float32), frame)
 
 
+@pytest.mark.parametrize("frame", [0, 1])
+def test_mc_write_pass_counts_again(ctx, frame):
+    """With no room for the per-block count table the write pass counts the
+    vertex versions again: the same exact vertex sets and statistics."""
+    import isosim
+    dims = (40, 33, 29)
+    vol = blobs(dims, 7) + 0.05 * np.random.default_rng(8).standard_normal(dims).astype(np.float32)
+    isos = np.linspace(vol.min(), vol.max(), 12)[1:-1].astype(np.float32)
+    c2 = isosim.Context(0)
+    try:
+        c2.set_surf_block_count_bytes(0)
+        check_mc(c2, vol, dims, isos, frame)
+    finally:
+        c2.close()
+
+
 def test_mc_integer_data_corner_vertices(ctx):
     """Isovalues equal to data values put vertices exactly on grid points that
     several edges share: the de-duplication must merge them."""
