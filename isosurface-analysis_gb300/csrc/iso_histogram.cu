@@ -105,7 +105,7 @@ __device__ __noinline__ int4 exact_bins4(float mn, float step, int bins, int rs,
 // (+0.0, all bits clear) the bucket is bits(lo) - bits(2^23).  One OR over the
 // bits of the eight sums of four voxels is 0 exactly when every pair of floors
 // agrees; a NaN value gives a NaN sum, whose bits are not 0.  Otherwise the
-// four voxels take the division, which happens for about 2^-20 * q of the
+// four voxels take the division, which happens for about 2^-21 * q of the
 // values.  Near q = bins the bucket is clamped to the last bin on both paths.
 constexpr float FLOOR_BASE = 8388608.0f;  // 2^23
 constexpr uint32_t FLOOR_BASE_BITS = 0x4B000000u;

@@ -119,7 +119,7 @@ def test_fast_path_agrees_with_division(bins):
         f0, a0 = bracket_bucket(np.array([mn], np.float32), mn, step, bins)
         assert f0[0] == 0 and not a0[0]
     assert kept > 100000
-    # the exact division is rare: about 2^-20 * q of random values plus edges
+    # the exact division is rare: about 2^-21 * q of random values plus edges
     assert flagged < 0.05 * kept
 
 
