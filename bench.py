@@ -158,8 +158,9 @@ def run_ours(args):
                        df_method=method, bins=bins, out=out)
 
     for _ in range(args.warmup):
-        _, ids, _, timing = step(d_vol, ism_dev)
+        _, ids, sstats, timing = step(d_vol, ism_dev)
     m = len(ids)
+    P = int(sum(sstats[k].points for k in range(len(isos))))  # surface points of all isovalues
     pairs = m * (m - 1) // 2
     torch.cuda.synchronize()
 
@@ -241,6 +242,17 @@ def run_ours(args):
                 "updates_per_s": round(updates, 1),
                 "stage_ms": {"surfaces": round(stage[0], 3), "distance_fields": round(stage[1], 3),
                              "histograms_nmi": round(stage[2], 3)}}
+    # the other stages against their own algorithmic work: surfaces 4 V bytes
+    # read (one pass over the volume for all isovalues) + 12 bytes per point
+    # written, against HBM; distance fields as queries/s and (sample, point)
+    # pairs/s (an exact search, latency-bound: not roofline-graded)
+    surf_bytes = 4.0 * F + 12.0 * P
+    roofline["stages"] = {
+        "surfaces": {"algorithmic_bytes": surf_bytes, "achieved_gbs": round(surf_bytes / (stage[0] / 1e3) / 1e9, 2),
+                     "frac_of_hbm": round(surf_bytes / (stage[0] / 1e3) / 1e9 / peak, 5), "points": P},
+        "distance_fields": {"queries_per_s": round(m * F / (stage[1] / 1e3), 1),
+                            "sample_point_pairs_per_s": round(float(F) * P / (stage[1] / 1e3), 1)},
+    }
 
     line = {
         "metric": METRIC if args.config == 3 else "ISM pairs/sec",
@@ -494,7 +506,7 @@ def run_multi(args):
     F = S ** 3
     stride = (F + 63) // 64 * 64
     ctx = isosim.Context(local)
-    stats = {"ism_pairs": 0, "t_ism": 0.0, "stage_ms": np.zeros(3)}
+    stats = {"ism_pairs": 0, "t_ism": 0.0, "stage_ms": np.zeros(3), "t_parts": np.zeros(3)}
 
     # this rank's volumes are generated before the timed batch (the engine's
     # input, like a volume loaded from disk)
@@ -508,16 +520,20 @@ def run_multi(args):
             vol = volumes[vid]
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            vmin, vmax = float(vol.min()), float(vol.max())
+            vmin, vmax = ctx.real_range(vol)  # the engine's device reduction
             isos = np.array([vmin + (i + 1) * (vmax - vmin) / (n + 1) for i in range(n)], np.float32)
+            t1 = time.perf_counter()
             ism, ids, _, timing = ctx.ism(vol, shape, isos, bins=bins)
+            t2 = time.perf_counter()
             stats["ism_pairs"] += len(ids) * (len(ids) - 1) // 2
             stats["stage_ms"] += [timing.surface_ms, timing.distance_ms, timing.histogram_ms]
             picks = sorted(r[3] for r in isosim.select_representatives(ism, ids, isos, reps))
             for q, row in enumerate(picks):
                 ctx.copy_field(row, rows[(vid - lo) * reps + q])
             torch.cuda.synchronize()
-            stats["t_ism"] += time.perf_counter() - t0
+            t3 = time.perf_counter()
+            stats["t_ism"] += t3 - t0
+            stats["t_parts"] += [t1 - t0, t2 - t1, t3 - t2]
         return rows
 
     R = V * T * reps
@@ -559,7 +575,10 @@ def run_multi(args):
                 "rank0_ism_stage": {"pairs": int(stats["ism_pairs"]), "seconds": round(stats["t_ism"], 3),
                                     "engine_stage_s": {k: round(float(v) / 1e3, 3) for k, v in
                                                        zip(("surfaces", "distance_fields", "histograms_nmi"),
-                                                           stats["stage_ms"])}},
+                                                           stats["stage_ms"])},
+                                    "host_s": {k: round(float(v), 3) for k, v in
+                                               zip(("isovalue_range", "ism_call", "representatives_and_copies"),
+                                                   stats["t_parts"])}},
                 "rank0_cross_stage": {"pairs": int(stats.get("cross_pairs", 0)),
                                       "seconds": round(stats.get("t_cross", 0.0), 3)},
                 "tsm_vsm_sample": {"first_blocks": [[int(a), int(b), round(float(x), 4), round(float(y), 4)]
