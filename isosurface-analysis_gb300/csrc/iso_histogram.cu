@@ -775,15 +775,25 @@ struct MiArgs {
     uint32_t *colrow_dump;
 };
 
-// One block per pair: marginals and sum(c ln c) of the global histogram, NMI.
-__global__ void __launch_bounds__(256) joint_mi_kernel(MiArgs a)
+// One block of MI_THREADS per pair: marginals and sum(c ln c) of the global
+// histogram, NMI.  FB: bins as a compile-time constant (0: a.bins).  With a
+// multiple of 32 bins a warp reads part of one row and one warp sum replaces
+// the row-sum atomics; with a divisor of the block size as bins every thread
+// reads a single column and sums it in a register.
+constexpr int MI_THREADS = 256;
+
+template <int FB>
+__global__ void __launch_bounds__(MI_THREADS) joint_mi_kernel(MiArgs a)
 {
     __shared__ uint32_t s_row[ISO_MAX_BINS], s_col[ISO_MAX_BINS];  // n < 2^32
-    __shared__ double s_red[3][8];
+    __shared__ double s_red[3][MI_THREADS / 32];
     const int p = blockIdx.x;
     const int2 task = a.tasks[p];
     const int i = task.x, j = task.y;
-    const int bins = a.bins;
+    const int bins = FB ? FB : a.bins;
+    const int lane = threadIdx.x & 31;
+    const bool warp_rows = (bins & 31) == 0;
+    const bool col_own = (MI_THREADS % bins) == 0;
     const uint32_t *gh = a.ghist + (size_t)p * bins * bins;
     for (int c = threadIdx.x; c < bins; c += blockDim.x) {
         s_row[c] = 0;
@@ -792,17 +802,60 @@ __global__ void __launch_bounds__(256) joint_mi_kernel(MiArgs a)
     __syncthreads();
     double hxy = 0.0;
     const bool dump = a.joint_dump != nullptr;
-    for (int idx = threadIdx.x; idx < bins * bins; idx += blockDim.x) {
+    uint32_t cs_own = 0;
+    if constexpr (FB == 256) {
+        // 128-bit loads of four bins: a warp reads half a row, and thread t
+        // always the columns 4 (t % 64) .. 4 (t % 64) + 3
+        static_assert((MI_THREADS * 4) % FB == 0, "one column group per thread");
+        const uint4 *gh4 = reinterpret_cast<const uint4 *>(gh);
+        uint4 cs4 = make_uint4(0u, 0u, 0u, 0u);
+        for (int q = threadIdx.x; q < FB * FB / 4; q += MI_THREADS) {
+            const uint4 c = __ldcs(gh4 + q);
+            const int r = q / (FB / 4), col = (q % (FB / 4)) * 4;
+            if (dump) {
+                const uint32_t cv[4] = {c.x, c.y, c.z, c.w};
+                for (int e = 0; e < 4; ++e) {
+                    a.joint_dump[(((size_t)i * a.m + j) * FB + r) * FB + col + e] = cv[e];
+                    if (a.symmetric && i != j) a.joint_dump[(((size_t)j * a.m + i) * FB + col + e) * FB + r] = cv[e];
+                }
+            }
+            if (c.x) hxy -= clnc_of(a.clnc, c.x);
+            if (c.y) hxy -= clnc_of(a.clnc, c.y);
+            if (c.z) hxy -= clnc_of(a.clnc, c.z);
+            if (c.w) hxy -= clnc_of(a.clnc, c.w);
+            const uint32_t rs = __reduce_add_sync(0xffffffffu, c.x + c.y + c.z + c.w);
+            if (lane == 0 && rs) atomicAdd(&s_row[r], rs);
+            cs4.x += c.x;
+            cs4.y += c.y;
+            cs4.z += c.z;
+            cs4.w += c.w;
+        }
+        const int col = (threadIdx.x % (FB / 4)) * 4;
+        if (cs4.x) atomicAdd(&s_col[col], cs4.x);
+        if (cs4.y) atomicAdd(&s_col[col + 1], cs4.y);
+        if (cs4.z) atomicAdd(&s_col[col + 2], cs4.z);
+        if (cs4.w) atomicAdd(&s_col[col + 3], cs4.w);
+    } else {
+    // bins^2 is a multiple of the block size whenever warp_rows holds, so all
+    // lanes of a warp run the same iterations for the warp sum
+    for (int idx = threadIdx.x; idx < bins * bins; idx += MI_THREADS) {
         const uint32_t c = gh[idx];
-        const int r = idx / bins, col = idx % bins;
+        const int r = idx / bins, col = idx - r * bins;
         if (dump) {
             a.joint_dump[(((size_t)i * a.m + j) * bins + r) * bins + col] = c;
             if (a.symmetric && i != j) a.joint_dump[(((size_t)j * a.m + i) * bins + col) * bins + r] = c;
         }
-        if (!c) continue;
-        hxy -= clnc_of(a.clnc, c);
-        atomicAdd(&s_row[r], c);
-        atomicAdd(&s_col[col], c);
+        if (c) hxy -= clnc_of(a.clnc, c);
+        if (warp_rows) {
+            const uint32_t rs = __reduce_add_sync(0xffffffffu, c);
+            if (lane == 0 && rs) atomicAdd(&s_row[r], rs);
+        } else if (c) {
+            atomicAdd(&s_row[r], c);
+        }
+        if (col_own) cs_own += c;
+        else if (c) atomicAdd(&s_col[col], c);
+    }
+    if (col_own && cs_own) atomicAdd(&s_col[threadIdx.x % bins], cs_own);
     }
     __syncthreads();
     double hx = 0.0, hy = 0.0;
@@ -821,7 +874,7 @@ __global__ void __launch_bounds__(256) joint_mi_kernel(MiArgs a)
             }
         }
     }
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         hxy += __shfl_xor_sync(0xffffffffu, hxy, o);
@@ -836,7 +889,7 @@ __global__ void __launch_bounds__(256) joint_mi_kernel(MiArgs a)
     __syncthreads();
     if (threadIdx.x == 0) {
         double sxy = 0.0, sy = 0.0, sx = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        for (int w = 0; w < MI_THREADS / 32; ++w) {
             sxy += s_red[0][w];
             sy += s_red[1][w];
             sx += s_red[2][w];
@@ -1064,7 +1117,7 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
             ma.ism = d_ism;
             ma.joint_dump = d_joint_dump;
             ma.colrow_dump = d_colrow_dump;
-            joint_mi_kernel<<<np, 256, 0, ctx->stream>>>(ma);
+            (bins == 256 ? joint_mi_kernel<256> : joint_mi_kernel<0>)<<<np, MI_THREADS, 0, ctx->stream>>>(ma);
             ISO_LAUNCHED(ctx);
         }
         return ISO_OK;
