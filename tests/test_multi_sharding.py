@@ -88,3 +88,16 @@ def test_cross_blocks_match_reference_loops():
         lo, hi = multi.shard(10, r, 3)
         assert 0 <= lo <= hi <= 10
     assert sum(multi.shard(10, r, 3)[1] - multi.shard(10, r, 3)[0] for r in range(3)) == 10
+
+
+def test_block_pairs_layout():
+    """Field pairs of each volume block, i major: block (a, b) gives rows
+    (a*reps + i, b*reps + j) in the order of two nested loops over i, j."""
+    from isosim import multi
+    blocks = multi.cross_blocks(3, 4)
+    reps = 5
+    want = [(a * reps + i, b * reps + j) for a, b in blocks for i in range(reps) for j in range(reps)]
+    got = multi.block_pairs(blocks, reps)
+    assert got.dtype == np.int32 and got.shape == (len(want), 2)
+    assert [tuple(p) for p in got.tolist()] == want
+    assert multi.block_pairs([], reps).shape == (0, 2)
