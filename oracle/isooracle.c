@@ -17,7 +17,7 @@
  *   - marching cubes, distance fields and representative selection are
  *     restatements of the reference's GPU/host code (no runnable reference
  *     counterpart exists in this environment); the FP64 distance field is the
- *     exact nearest-surface distance they are judged against.
+ *     exact nearest-surface distance they are compared against.
  *
  * Compile with -ffp-contract=off: every rounding step is written out explicitly
  * (fmaf where a fused multiply-add is meant), so x86-64 and aarch64 builds give
