@@ -41,8 +41,19 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
+def load_synth():
+    """The synthetic-volume generators, loaded from their file: importing the
+    isosim package would load the engine's library, which the reference arm
+    must not have in its process."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("iso_bench_synth", os.path.join(PKG, "isosim", "synth.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def workload(config):
-    import isosim.synth as synth
+    synth = load_synth()
     if config == 1:
         vol, isos, bins = synth.config1()
         name = "64^3 8-blob volume, 32 isovalues, 128 bins"
@@ -53,6 +64,13 @@ def workload(config):
         vol, isos, bins = synth.config3()
         name = "256^3 12-blob + 0.05 k^-2 noise volume, 256 isovalues, 256 bins"
     return vol, isos, bins, name
+
+
+def bench_config(args, name, n, bins, world):
+    """The workload description both arms print (identical for equal flags)."""
+    return {"workload": name, "isovalues": int(n), "bins": int(bins), "pairs_per_ism": int(n * (n - 1) // 2),
+            "l2": "256 MB flush before every timed step",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
 class ClockSampler:
@@ -217,17 +235,15 @@ def run_ours(args):
     achieved = hist_bytes / hist_s / 1e9
     counter_peak = ctx.counter_rate(bins if bins & (bins - 1) == 0 else 256)
     updates = F * pairs / hist_s
-    # DRAM traffic of the histogram stage: --hist-traffic, else a one-pass ncu
-    # capture (dram__bytes_read.sum + dram__bytes_write.sum) of the default
-    # 256^3 workload with the segment-major schedule (9 chunks: 9 segment-kernel
-    # and 9 NMI-kernel launches, summed); other schedules report null
+    # DRAM traffic of the histogram stage: --hist-traffic, else the committed
+    # ncu summary of this workload when it was captured on the current
+    # histogram source; otherwise null
     traffic, traffic_src = args.hist_traffic, "--hist-traffic"
     if traffic is None and args.config == 3 and bins == 256 and seg_values == 2097152:
-        traffic = 7.9575e11 + 11.372e9 + 8.6476e9 + 1.8e6
-        traffic_src = "ncu capture of this workload (18 launches of the stage, 431 ms)"
+        traffic, traffic_src = histogram_traffic()
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 5), "traffic": traffic,
-                "traffic_source": traffic_src if traffic is not None else None,
+                "traffic_source": traffic_src,
                 "traffic_over_unique": round(traffic / hist_bytes, 1) if traffic else None,
                 "kernel": ("joint_histogram_wide_kernel" if bins <= 224 else
                            ("joint_histogram_seg_kernel + joint_mi_kernel" if 0 < seg_values < F
@@ -267,23 +283,89 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "f32 (FP64 NMI)",
         "data": "synthetic (seeded)",
-        "config": {"workload": name, "isovalues": int(n), "nonempty_surfaces": int(m), "pairs": int(pairs),
-                   "bins": int(bins), "surface": "marching cubes (reference frame)",
-                   "distance": args.df, "l2": "256 MB flush before every timed step",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": bench_config(args, name, n, bins, world),
+        "method": {"surface": "marching cubes (reference frame)", "distance": args.df, "mi": "FP64",
+                   "nonempty_surfaces": int(m), "pairs": int(pairs)},
         "e2e": {"value": round(world * pairs / (e2e_ms / 1e3), 2), "unit": "pairs/s",
                 "h2d_bytes_per_step": int(F * 4 + n * 4), "d2h_bytes_per_step": int(m * m * 4 + m * 4)},
         "gpu_launches": int(launches),
         "roofline": roofline,
         "clocks": clocks,
     }
+    if rank == 0 and not args.no_plain:
+        line["plain"] = plain_leg(ctx, vol, isos, sstats, stage, pairs, value, args.plain_surfaces)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(vol, isos, bins, sample_scale=args.cpu_scale)
+    if rank == 0 and args.serving_requests > 0:
+        ctx.close()
+        ctx = None
+        batched, one, desc = serving_stats(args.serving_requests, args.rate, args.slots, args.budget_gb)
+        line["serving"] = {"workload": desc, "continuous_batching": batched, "one_at_a_time": one}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
+    if ctx is not None:
+        ctx.close()
     if pg is not None:
         pg.destroy_process_group()
+
+
+TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "histogram_traffic__ism-256cubed-256iso-256bins.md")
+HIST_SOURCE = os.path.join(PKG, "csrc", "iso_histogram.cu")
+
+
+def histogram_traffic():
+    """(DRAM bytes of the histogram stage per ISM, source) from the committed
+    ncu summary, which records the sha256 of csrc/iso_histogram.cu it was
+    captured on; (None, reason) when it is absent or that source changed."""
+    import hashlib
+    if not os.path.exists(TRAFFIC_PROFILE):
+        return None, "no ncu summary committed for this workload"
+    vals = {}
+    with open(TRAFFIC_PROFILE) as f:
+        for line in f:
+            if ":" in line and line.strip().startswith("- `"):
+                k, v = line.strip()[3:].split("`", 1)
+                vals[k] = v.split(":", 1)[1].strip().strip("`")
+    with open(HIST_SOURCE, "rb") as f:
+        sha = hashlib.sha256(f.read()).hexdigest()
+    if vals.get("source_sha256") != sha:
+        return None, "ncu summary was captured on another histogram source"
+    return float(vals["traffic_bytes_per_ism"]), "ncu capture (%s)" % os.path.relpath(TRAFFIC_PROFILE, ROOT)
+
+
+def plain_leg(ctx, vol, isos, sstats, stage, pairs, value, k_surfaces):
+    """The plain single-launch FP32 GPU path: the same surfaces and histograms,
+    with each distance field computed by brute force on the CUDA cores
+    (df_brute_kernel: every sample against every surface point).  The brute
+    force over all n surfaces takes minutes at 256^3, so it runs on
+    k_surfaces sampled surfaces and is scaled to the whole ISM by
+    (sample, point) pairs -- the brute force's work is exactly F*P per surface."""
+    import isosim
+    dims = vol.shape
+    F = int(np.prod(dims))
+    n = len(isos)
+    counts = np.array([sstats[k].points for k in range(n)], np.int64)
+    nonempty = np.nonzero(counts)[0]
+    pick = nonempty[np.linspace(len(nonempty) // 4, 3 * len(nonempty) // 4, k_surfaces).astype(int)]
+    pts, _ = ctx.surface_points(vol.ravel(), dims, isos[pick], surface=isosim.SURFACE_MC, frame=isosim.FRAME_REF)
+    work, secs = 0.0, 0.0
+    for p in pts:
+        pn = (p / np.float32(max(dims))).astype(np.float32)
+        ctx.distance_field(pn[:64], dims, method=isosim.DF_BRUTE)  # warm-up
+        t0 = time.perf_counter()
+        ctx.distance_field(pn, dims, method=isosim.DF_BRUTE)
+        secs += time.perf_counter() - t0
+        work += float(F) * len(p)
+    rate = work / secs
+    df_s = float(F) * float(counts.sum()) / rate
+    t_ism = (stage[0] + stage[2]) / 1e3 + df_s
+    plain = pairs / t_ism
+    return {"value": round(plain, 2), "unit": "pairs/s", "extrapolated": True,
+            "distance": "brute-force FP32 (df_brute_kernel)", "seconds_per_ism": round(t_ism, 2),
+            "sample": "%d of %d surfaces (%d points) timed by brute force, %.3g (sample, point) pairs/s, scaled to "
+                      "all %d surface points; surfaces and histograms as measured above"
+                      % (len(pts), len(nonempty), int(sum(len(p) for p in pts)), rate, int(counts.sum())),
+            "batched_over_plain": round(value / plain, 1)}
 
 
 def cpu_baseline(vol, isos, bins, sample_scale=1.0):
@@ -352,35 +434,45 @@ def cpu_baseline(vol, isos, bins, sample_scale=1.0):
 
 
 def run_reference(args):
+    """The reference arm: the pipeline's arithmetic on the host cores (the
+    CPU restatements under oracle/: the reference's own compiled parts do not
+    build on the GPU host), never the engine.  Each step is one bounded
+    sample of the workload (cpu_baseline); ms_per_step is that sample's real
+    duration and value the sample's per-unit rates scaled to whole ISMs."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     vol, isos, bins, name = workload(args.config)
-    vals = []
+    n = len(isos)
     for _ in range(args.warmup):
-        cpu_baseline(vol, isos, bins, sample_scale=0.5)
+        cpu_baseline(vol, isos, bins, sample_scale=args.ref_scale)
+    vals, secs = [], []
     for _ in range(args.steps):
-        vals.append(cpu_baseline(vol, isos, bins, sample_scale=0.5))
+        t0 = time.perf_counter()
+        vals.append(cpu_baseline(vol, isos, bins, sample_scale=args.ref_scale))
+        secs.append(time.perf_counter() - t0)
     v = float(np.median([c["value"] for c in vals]))
     cb = dict(vals[0])
     cb["value"] = round(v, 4)
     line = {"metric": METRIC if args.config == 3 else "ISM pairs/sec", "value": round(v, 4), "unit": "pairs/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(1e3 * (len(isos) * (len(isos) - 1) // 2) / v, 1),
+            "ms_per_step": round(1e3 * float(np.mean(secs)), 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded)", "impl": "reference",
-            "config": {"workload": name, "note": "host cores; reference arithmetic; extrapolated from a sample"},
+            "data": "synthetic (seeded)", "impl": "reference", "extrapolated": True,
+            "step": "one bounded sample per step: " + cb["sample"],
+            "config": bench_config(args, name, n, bins, world),
             "cpu_baseline": cb,
             "e2e": {"value": round(v, 4), "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def run_serving(args):
+def serving_stats(requests, rate, slots, budget_gb):
     """Poisson stream of ISM requests through the serving loop (continuous
     batching under an HBM budget) and through one-request-at-a-time serving.
     Shapes, isovalue counts and bins are drawn per request (seeded); volumes
-    come from a small pool of seeded blob and k^-3 fields kept on the device."""
+    come from a small pool of seeded blob and k^-3 fields kept on the device.
+    Returns (batched, one_at_a_time, workload description)."""
     import torch
 
     import isosim
@@ -397,8 +489,8 @@ def run_serving(args):
             pool[(sh, "grf")] = torch.from_numpy(synth.power_law_field(sh, 3.0, 5200 + k).ravel()).cuda()
     reqs = []
     t = 0.0
-    for r in range(args.requests):
-        t += rng.exponential(1.0 / args.rate)
+    for r in range(requests):
+        t += rng.exponential(1.0 / rate)
         sh = shapes[rng.integers(len(shapes))]
         kind = "grf" if (sh, "grf") in pool and rng.random() < 0.5 else "blobs"
         n = int(rng.choice([16, 32, 64, 128, 256]))
@@ -412,7 +504,7 @@ def run_serving(args):
         reqs.append((t, vol, sh, isos, bins))
 
     def serve(slots):
-        with isosim.Server(0, slots=slots, budget_bytes=int(args.budget_gb * (1 << 30))) as srv:
+        with isosim.Server(0, slots=slots, budget_bytes=int(budget_gb * (1 << 30))) as srv:
             # warm each worker's arena on a small request
             for _ in range(slots):
                 srv.wait(srv.submit(pool[(shapes[0], "blobs")], shapes[0], reqs[0][3][:16], bins=128))
@@ -439,13 +531,18 @@ def run_serving(args):
                 "p50_ms": round(float(np.percentile(lat, 50)), 1), "p99_ms": round(float(np.percentile(lat, 99)), 1),
                 "peak_admitted_gb": round(st.peak_device_bytes / (1 << 30), 2)}
 
-    batched = serve(args.slots)
+    batched = serve(slots)
     plain = serve(1)
+    desc = ("Poisson stream of %d requests at %g req/s; shapes %s; isovalues {16..256}; bins {128,256}; "
+            "%g GB HBM budget; %d slots" % (requests, rate, shapes, budget_gb, slots))
+    return batched, plain, desc
+
+
+def run_serving(args):
+    batched, plain, desc = serving_stats(args.requests, args.rate, args.slots, args.budget_gb)
     line = {"metric": "ISM pairs/sec and p50/p99 latency, serving", "value": batched["pairs_per_s"],
             "unit": "pairs/s", "n_gpus": 1, "higher_is_better": True, "data": "synthetic (seeded)",
-            "config": {"workload": "Poisson stream of %d requests at %g req/s; shapes %s; isovalues {16..256}; "
-                                   "bins {128,256}; %g GB HBM budget" % (args.requests, args.rate, shapes, args.budget_gb),
-                       "slots": args.slots},
+            "config": {"workload": desc, "slots": args.slots},
             "continuous_batching": batched, "one_at_a_time": plain}
     print(json.dumps(line), flush=True)
 
@@ -632,6 +729,12 @@ def main():
     ap.add_argument("--hist-traffic", type=float, default=None,
                     help="DRAM bytes per histogram launch from an ncu capture (reported as roofline.traffic)")
     ap.add_argument("--cpu-scale", type=float, default=1.0)
+    ap.add_argument("--ref-scale", type=float, default=0.5,
+                    help="sample size of each reference-arm step (see cpu_baseline)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the brute-force plain-path leg")
+    ap.add_argument("--plain-surfaces", type=int, default=2)
+    ap.add_argument("--serving-requests", type=int, default=24,
+                    help="requests of the serving leg in the default line (0: none)")
     ap.add_argument("--case", default=None, choices=["hist-small", "pipe-small", "ism-128"],
                     help="run a small fixed case twice and exit (profiling target)")
     ap.add_argument("--mode", default="single", choices=["single", "serving", "multi"])

@@ -118,7 +118,27 @@ ISO_API int64_t iso_ctx_launches(iso_ctx *ctx);
                                                its count and write passes while that table takes at
                                                most this many bytes (default 2^30), else the write
                                                pass counts again; 0 = always count again */
+#define ISO_LIMIT_MI_MODE 4 /* ISO_MI_*: how the mutual information of a pair is computed
+                                (default ISO_MI_FP64; the reference-named entry points use
+                                ISO_MI_REF32) */
 ISO_API int iso_ctx_set_limit(iso_ctx *ctx, int which, int64_t value);
+
+/* Mutual-information modes (ISO_LIMIT_MI_MODE).  Both use the same exact
+ * joint histograms and the reference's formula ISM = 2I/(hX+hY) on raw counts.
+ *   ISO_MI_FP64:  FP64 sums, one value per unordered pair written to (i,j)
+ *                 and (j,i): the map is symmetric and accurate to float
+ *                 rounding of the FP64 result.
+ *   ISO_MI_REF32: the reference's own FP32 evaluation
+ *                 (isosurfaces_cuda/src/JointHistogram.cu:24-60, called once
+ *                 per ordered pair at :156-160): same summation order, logf
+ *                 and multiply-add contraction, so every entry equals the
+ *                 reference's bit for bit and (i,j) may differ from (j,i).
+ *                 Keeps all m*m joint histograms in device memory
+ *                 (m*m*bins*bins*4 bytes).  Applies to iso_ism,
+ *                 iso_similarity_map, iso_cross_map and calculate_histogram_h;
+ *                 iso_pair_map and iso_similarity_map_noalloc are FP64 only. */
+#define ISO_MI_FP64 0
+#define ISO_MI_REF32 1
 
 /* ---------------------------------------------------------------------- */
 /* Whole-volume pipeline (replaces the per-isovalue loop of Single::run,   */
@@ -223,6 +243,12 @@ ISO_API int iso_transpose_xfastest(iso_ctx *ctx, const float *src, int X, int Y,
  * fields the single module writes as distancefield-<k>.df. */
 ISO_API int iso_copy_field(iso_ctx *ctx, int row, float *out);
 
+/* Copies the joint histogram of ordered pair (i, j) (row = bucket of field i)
+ * kept by the context's last ISO_MI_REF32 similarity run (iso_ism,
+ * iso_similarity_map or iso_cross_map) to out (host or device, bins*bins
+ * uint32).  ISO_ERR_ARG when no histograms are kept. */
+ISO_API int iso_copy_joint_histogram(iso_ctx *ctx, int i, int j, uint32_t *out);
+
 /* Measures the peak rate of the joint-histogram kernel's counter update on
  * its own (packed 16-bit shared-memory atomic plus wrap check, random bins,
  * no bucket arithmetic or loads): the shared-memory-atomic roofline of the
@@ -239,8 +265,9 @@ typedef struct iso_int3 { int32_t x, y, z; } iso_int3;
  * and meaning: numFields fields (2*numFields with multi), similarity map
  * h_simMap (simMapSize x simMapSize), per-ordered-pair column and row sums
  * (numFields^2 * histogramSize each).  h_jointHist is left untouched, as the
- * reference leaves it (its copy-back is commented out, :397).  MI is FP64.
- * Uses a process-wide context on device 0. */
+ * reference leaves it (its copy-back is commented out, :397).  The map is the
+ * reference's FP32 MI, bit for bit (ISO_MI_REF32).  Runs on the calling
+ * thread's current CUDA device, through a process-wide context per device. */
 ISO_API void calculate_histogram_h(float **distanceFields, float *minValues, float *maxValues, const int fieldSize,
                                    const unsigned long numFields, const unsigned long histogramSize,
                                    unsigned int *h_jointHist, unsigned int *h_colSums, unsigned int *h_rowSums,
@@ -338,8 +365,9 @@ ISO_API void iso_server_destroy(iso_server *s);
  *             multiple of 4);  d_ism_out: m*m floats of device memory;
  *   stream:   a cudaStream_t (NULL = legacy default stream); the call
  *             synchronises it before returning.
- * Limits: m <= ISO_NOALLOC_MAX_FIELDS, n <= ISO_NOALLOC_MAX_VALUES, bins even
- * in [2, 256]; larger sizes return ISO_ERR_CAPACITY.  The first call on a
+ * Limits: m <= ISO_NOALLOC_MAX_FIELDS and n <= ISO_NOALLOC_MAX_VALUES (larger
+ * m or n return ISO_ERR_CAPACITY); bins even in [2, 256], a bad stride or
+ * alignment, or host pointers return ISO_ERR_ARG.  The first call on a
  * device looks up the array's device address and fills a lookup table, so
  * make it before any stream capture.  All calls share the array: calls that
  * overlap on the GPU race. */

@@ -26,6 +26,7 @@ SOURCES = [
     "iso_surface.cu",
     "iso_distance.cu",
     "iso_histogram.cu",
+    "iso_mi_ref32.cu",
     "iso_pipeline.cu",
     "iso_server.cu",
     "iso_multi.cu",
@@ -42,6 +43,18 @@ COMMON = [
     "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
     "-I", os.path.join(ROOT, "include"), "-I", CSRC,
 ]
+
+
+# Files compiled with nvcc's default multiply-add contraction instead of
+# -fmad=false: the reference-order FP32 MI must fuse exactly where the
+# reference's kernel does (its build passes no -fmad flag).
+DEFAULT_CONTRACTION = {"iso_mi_ref32.cu"}
+
+
+def flags_for(src):
+    if src in DEFAULT_CONTRACTION:
+        return [f for f in COMMON if f not in ("-fmad=false",)]
+    return COMMON
 
 
 def nvcc():
@@ -64,9 +77,9 @@ def _compile(src, force):
     obj = os.path.join(OBJ, src + ".o")
     if not force and not _stale(path, obj):
         return obj, None
-    cmd = [nvcc()] + COMMON + ARCH + ["-c", path, "-o", obj]
+    cmd = [nvcc()] + flags_for(src) + ARCH + ["-c", path, "-o", obj]
     if src.endswith(".cpp"):
-        cmd = [nvcc(), "-x", "cu"] + COMMON + ARCH + ["-c", path, "-o", obj]
+        cmd = [nvcc(), "-x", "cu"] + flags_for(src) + ARCH + ["-c", path, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         return obj, "compile failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr)

@@ -2,6 +2,7 @@
 #include <cstdarg>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 
 #include "iso_internal.cuh"
@@ -66,6 +67,7 @@ void iso_ctx_release(iso_ctx *ctx)
     }
     ctx->clnc_ready = false;
     ctx->last_m = 0;
+    ctx->joint_m = 0;
 }
 
 void iso_ctx_release_except_surfaces(iso_ctx *ctx)
@@ -83,6 +85,7 @@ void iso_ctx_release_except_surfaces(iso_ctx *ctx)
     }
     ctx->clnc_ready = false;
     ctx->last_m = 0;
+    ctx->joint_m = 0;
 }
 
 extern "C" int iso_ctx_set_limit(iso_ctx *ctx, int which, int64_t value)
@@ -101,6 +104,11 @@ extern "C" int iso_ctx_set_limit(iso_ctx *ctx, int which, int64_t value)
     case ISO_LIMIT_SURF_BLOCK_COUNT_BYTES:
         if (value < 0) return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: byte limit must be >= 0");
         ctx->surf_block_count_bytes = value;
+        return ISO_OK;
+    case ISO_LIMIT_MI_MODE:
+        if (value != ISO_MI_FP64 && value != ISO_MI_REF32)
+            return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: unknown MI mode %lld", (long long)value);
+        ctx->mi_mode = (int)value;
         return ISO_OK;
     default:
         return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: unknown limit %d", which);
@@ -178,13 +186,25 @@ bool iso_is_device_ptr(const void *p)
 }
 
 static std::mutex g_default_mu;
-static iso_ctx *g_default_ctx = nullptr;
+static std::map<int, iso_ctx *> g_default_ctx;  // one per device, kept until exit
 
 iso_ctx *iso_default_ctx()
 {
-    std::lock_guard<std::mutex> lock(g_default_mu);
-    if (!g_default_ctx) {
-        if (iso_ctx_create(0, &g_default_ctx) != ISO_OK) g_default_ctx = nullptr;
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) {
+        cudaGetLastError();
+        iso_fail(ISO_ERR_CUDA, "no current CUDA device");
+        return nullptr;
     }
-    return g_default_ctx;
+    std::lock_guard<std::mutex> lock(g_default_mu);
+    iso_ctx *&c = g_default_ctx[device];
+    if (!c) {
+        if (iso_ctx_create(device, &c) != ISO_OK) {
+            c = nullptr;
+            return nullptr;
+        }
+        // the reference-named entry points return the reference's own numbers
+        c->mi_mode = ISO_MI_REF32;
+    }
+    return c;
 }

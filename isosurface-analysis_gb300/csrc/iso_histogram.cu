@@ -1026,9 +1026,24 @@ int iso_run_similarity(iso_ctx *ctx, const float *d_fields_a, const float *d_fie
     std::vector<int2> h_tasks(max_tasks);
     int num_tasks = 0;
     build_tasks(m, symmetric, h_tasks.data(), &num_tasks);
-    return iso_run_similarity_tasks(ctx, d_fields_a, symmetric ? d_fields_a : d_fields_b, m, n, stride, bins, d_minmax_a,
-                                    symmetric ? d_minmax_a : d_minmax_b, d_ism, h_tasks.data(), num_tasks,
-                                    symmetric, d_joint_dump, d_colrow_dump);
+    if (ctx->mi_mode == ISO_MI_REF32 && !d_joint_dump) {
+        // the reference's FP32 MI walks every ordered pair's histogram: keep them all
+        void *p;
+        ISO_TRY(iso_buf(ctx, BUF_HIST_DUMP, (size_t)m * m * bins * bins * sizeof(uint32_t), &p));
+        d_joint_dump = (uint32_t *)p;
+    }
+    ISO_TRY(iso_run_similarity_tasks(ctx, d_fields_a, symmetric ? d_fields_a : d_fields_b, m, n, stride, bins,
+                                     d_minmax_a, symmetric ? d_minmax_a : d_minmax_b, d_ism, h_tasks.data(), num_tasks,
+                                     symmetric, d_joint_dump, d_colrow_dump));
+    ctx->joint_m = 0;
+    if (ctx->mi_mode == ISO_MI_REF32) {
+        ISO_TRY(iso_run_mi_ref32(ctx, d_joint_dump, m, bins, n, d_ism));
+        if (d_joint_dump == (uint32_t *)ctx->buf[BUF_HIST_DUMP]) {
+            ctx->joint_m = m;
+            ctx->joint_bins = bins;
+        }
+    }
+    return ISO_OK;
 }
 
 int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float *d_fields_b, int m, int64_t n,

@@ -110,6 +110,10 @@ struct iso_ctx {
     int64_t lbvh_group_points = ISO_LBVH_GROUP_POINTS;  // see iso_ctx_set_limit
     int64_t hist_segment_values = ISO_HIST_SEGMENT_VALUES;  // 0: one CTA per pair for every length
     int64_t surf_block_count_bytes = ISO_SURF_BLOCK_COUNT_BYTES;  // see iso_ctx_set_limit
+    int mi_mode = ISO_MI_FP64;  // ISO_MI_*: precision and order of the mutual information
+    // joint histograms of all ordered pairs kept in BUF_HIST_DUMP by the last
+    // ISO_MI_REF32 similarity run (0 = none)
+    int joint_m = 0, joint_bins = 0;
     int (*admit)(void *user, size_t bytes) = nullptr;
     void *admit_user = nullptr;
     // request shape for the admission estimate (set by iso_ism)
@@ -129,7 +133,8 @@ int iso_buf(iso_ctx *ctx, IsoBuf b, size_t bytes, void **out);
 // Pinned host scratch of at least `bytes`.
 int iso_host_scratch(iso_ctx *ctx, size_t bytes, void **out);
 
-// Process-wide context for the reference-named entry points.
+// Process-wide context of the calling thread's current device, for the
+// reference-named entry points (created on first use, reference FP32 MI).
 iso_ctx *iso_default_ctx();
 
 // True if `p` is a device (or managed) pointer.
@@ -175,5 +180,9 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
                              float *d_ism, const int2 *h_tasks, int64_t num_tasks, bool symmetric,
                              uint32_t *d_joint_dump, uint32_t *d_colrow_dump);
 int iso_run_minmax(iso_ctx *ctx, const float *d_fields, int m, int64_t n, int64_t stride, uint32_t *d_minmax);
+// The reference's FP32 MI (calculateMutualInformation, summation order and
+// contraction included) of all m*m ordered pairs whose joint histograms are at
+// d_joint (pair i*m + j at d_joint + (i*m + j)*bins*bins), into d_ism[i*m + j].
+int iso_run_mi_ref32(iso_ctx *ctx, const uint32_t *d_joint, int m, int bins, int64_t n, float *d_ism);
 
 constexpr int ISO_MAX_ISOVALUES = 4096;

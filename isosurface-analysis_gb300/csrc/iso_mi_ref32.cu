@@ -1,0 +1,116 @@
+// iso_mi_ref32.cu -- the reference's FP32 mutual information, reproduced bit for
+// bit on the GPU (opt-in: ISO_MI_REF32; the default of the reference-named
+// entry points).
+//
+// The reference evaluates calculateMutualInformation
+// (isosurfaces_cuda/src/JointHistogram.cu:24-60) on the device, inside
+// calculate_histogram_g (:156-160), once per ORDERED pair (i, j): one thread
+// walks the pair's joint histogram row by row in FP32, with logf and the
+// compiler's default multiply-add contraction.  Its map is therefore not
+// symmetric, and it differs from an accurate MI by its own rounding (about
+// 7e-5 on 64^3 fields at 128 bins).  A caller who needs the reference's numbers
+// (the drop-in calculate_histogram_h) gets them from this kernel.
+//
+// This file is compiled WITHOUT -fmad=false (nvcc's default contraction, as
+// the reference's build uses), so that each accumulation below compiles to the
+// same fused operation as the reference's; every other file of the engine
+// forbids contraction.
+//
+// Layout: joint histograms of all m*m ordered pairs, pair q = i*m + j at
+// joint + q*bins*bins, row = bucket of field i (the histogram kernels' dump).
+// One warp walks 32 pairs, one lane per pair: it stages 32 consecutive bins of
+// each of its pairs in shared memory with coalesced loads (adding them into
+// per-pair column sums there), then each lane continues its pair's serial sums
+// over the staged bins.  Row sums are formed by the walking lane at each row
+// end; column sums are summed once the walk is done.  The order of every
+// summation chain is the reference's.
+#include "iso_internal.cuh"
+
+namespace {
+
+constexpr int R32_PAIRS = 32;  // ordered pairs per CTA (one warp, one lane per pair)
+constexpr int R32_TILE = 32;   // bins of each pair staged per step
+
+// The reference's per-bin term h -= c * logf(c) for a nonzero count.  Kept as
+// one expression so that the compiler fuses the product into the subtraction
+// exactly as it does in the reference's kernel.
+__device__ __forceinline__ float entropy_step(float h, uint32_t count)
+{
+    float c = (float)count;
+    h -= c * logf(c);
+    return h;
+}
+
+__global__ void __launch_bounds__(R32_PAIRS) mi_ref32_kernel(const uint32_t *__restrict__ joint, int64_t num_pairs,
+                                                            int bins, float num_values, float *__restrict__ ism)
+{
+    extern __shared__ uint32_t smem[];
+    uint32_t *tile = smem;                                     // [R32_PAIRS][R32_TILE + 1]
+    uint32_t *colsum = smem + R32_PAIRS * (R32_TILE + 1);      // [R32_PAIRS][bins]
+    const int lane = threadIdx.x;
+    const int64_t first = (int64_t)blockIdx.x * R32_PAIRS;
+    const int64_t hist = (int64_t)bins * bins;
+    for (int k = lane; k < R32_PAIRS * bins; k += R32_PAIRS) colsum[k] = 0;
+    __syncwarp();
+
+    float hXY = 0.0f, hY = 0.0f;
+    uint32_t row_sum = 0;
+    int col = 0;
+    for (int64_t k0 = 0; k0 < hist; k0 += R32_TILE) {
+        // stage bins k0 .. k0+31 of every pair of this CTA (128 B per pair)
+        const int64_t k = k0 + lane;
+        const int kcol = (int)(k % bins);
+#pragma unroll 4
+        for (int p = 0; p < R32_PAIRS; ++p) {
+            uint32_t v = 0;
+            if (first + p < num_pairs && k < hist) v = __ldcs(joint + (first + p) * hist + k);
+            tile[p * (R32_TILE + 1) + lane] = v;
+            if (v) atomicAdd(&colsum[p * bins + kcol], v);
+        }
+        __syncwarp();
+        // this lane's pair: the reference's row-major walk over the staged bins
+        const int steps = hist - k0 < R32_TILE ? (int)(hist - k0) : R32_TILE;
+        for (int s = 0; s < steps; ++s) {
+            const uint32_t v = tile[lane * (R32_TILE + 1) + s];
+            if (v > 0) hXY = entropy_step(hXY, v);
+            row_sum += v;
+            if (++col == bins) {
+                if (row_sum > 0) hY = entropy_step(hY, row_sum);
+                row_sum = 0;
+                col = 0;
+            }
+        }
+        __syncwarp();
+    }
+    if (first + lane >= num_pairs) return;
+    float hX = 0.0f;
+    for (int c = 0; c < bins; ++c) {
+        const uint32_t v = colsum[lane * bins + c];
+        if (v > 0) hX = entropy_step(hX, v);
+    }
+    // JointHistogram.cu:53-59, operation for operation
+    hXY = hXY / num_values + logf(num_values);
+    hX = hX / num_values + logf(num_values);
+    hY = hY / num_values + logf(num_values);
+    float iXY = hX + hY - hXY;
+    float val = 2 * iXY / (hX + hY);
+    ism[first + lane] = val != val ? 0.0f : val;
+}
+
+}  // namespace
+
+// Reference-order FP32 MI of all m*m ordered pairs whose joint histograms are
+// at d_joint (pair i*m + j, row = bucket of field i); n = values per field.
+int iso_run_mi_ref32(iso_ctx *ctx, const uint32_t *d_joint, int m, int bins, int64_t n, float *d_ism)
+{
+    if (m <= 0) return ISO_OK;
+    const int64_t pairs = (int64_t)m * m;
+    const int64_t ctas = (pairs + R32_PAIRS - 1) / R32_PAIRS;
+    if (ctas > 0x7fffffff) return iso_fail(ISO_ERR_ARG, "reference FP32 MI: too many pairs");
+    const size_t smem = ((size_t)R32_PAIRS * (R32_TILE + 1) + (size_t)R32_PAIRS * bins) * sizeof(uint32_t);
+    // the reference converts its int field size to float (JointHistogram.cu:24, :159)
+    const float nv = (float)n;
+    mi_ref32_kernel<<<(unsigned)ctas, R32_PAIRS, smem, ctx->stream>>>(d_joint, pairs, bins, nv, d_ism);
+    ISO_LAUNCHED(ctx);
+    return ISO_OK;
+}

@@ -507,6 +507,23 @@ extern "C" int iso_copy_field(iso_ctx *ctx, int row, float *out)
     return ISO_OK;
 }
 
+extern "C" int iso_copy_joint_histogram(iso_ctx *ctx, int i, int j, uint32_t *out)
+{
+    iso_clear_error();
+    if (!ctx || !out) return iso_fail(ISO_ERR_ARG, "iso_copy_joint_histogram: bad argument");
+    const int m = ctx->joint_m, bins = ctx->joint_bins;
+    if (m <= 0 || !ctx->buf[BUF_HIST_DUMP])
+        return iso_fail(ISO_ERR_ARG, "iso_copy_joint_histogram: no histograms kept (run a map in ISO_MI_REF32 mode)");
+    if (i < 0 || j < 0 || i >= m || j >= m)
+        return iso_fail(ISO_ERR_ARG, "iso_copy_joint_histogram: pair (%d, %d) outside %d x %d", i, j, m, m);
+    ISO_CUDA(cudaSetDevice(ctx->device));
+    const size_t h = (size_t)bins * bins;
+    ISO_CUDA(cudaMemcpyAsync(out, (const uint32_t *)ctx->buf[BUF_HIST_DUMP] + ((size_t)i * m + j) * h,
+                             h * sizeof(uint32_t), cudaMemcpyDefault, ctx->stream));
+    ISO_CUDA(cudaStreamSynchronize(ctx->stream));
+    return ISO_OK;
+}
+
 // ---------------------------------------------------------------------------
 // reference-named drop-in functions
 // ---------------------------------------------------------------------------

@@ -26,6 +26,8 @@ FRAME_REF = 0
 FRAME_CANON = 1
 DF_BRUTE = 0
 DF_LBVH = 1
+MI_FP64 = 0
+MI_REF32 = 1
 MC_REF_DROPPED = 1
 
 
@@ -100,6 +102,7 @@ def _load():
         "iso_generate_hierarchy_h": (C.c_int, [P, C.c_long, C.c_int, C.c_int, C.c_int, P, C.c_int, C.c_int]),
         "iso_transpose_xfastest": (C.c_int, [P, P, C.c_int, C.c_int, C.c_int, P]),
         "iso_copy_field": (C.c_int, [P, C.c_int, P]),
+        "iso_copy_joint_histogram": (C.c_int, [P, C.c_int, C.c_int, P]),
         "iso_server_create": (C.c_int, [C.c_int, C.c_int, C.c_size_t, C.POINTER(P)]),
         "iso_server_submit": (C.c_int, [P, C.POINTER(Request), C.POINTER(C.c_int64)]),
         "iso_server_wait": (C.c_int, [P, C.c_int64, C.POINTER(RequestResult)]),
@@ -183,6 +186,11 @@ class Context:
         """Fields longer than `values` use the segment-major histogram schedule (0: never)."""
         _check(lib.iso_ctx_set_limit(self.handle, 2, int(values)))
 
+    def set_mi_mode(self, mode):
+        """MI_FP64 (default: accurate, symmetric) or MI_REF32 (the reference's
+        own FP32 evaluation per ordered pair, bit for bit)."""
+        _check(lib.iso_ctx_set_limit(self.handle, 4, int(mode)))
+
     def set_surf_block_count_bytes(self, nbytes):
         """Largest per-block vertex-count table marching cubes keeps between its
         passes (0: the write pass counts again)."""
@@ -257,6 +265,12 @@ class Context:
     def copy_field(self, row, out):
         """Row `row` of the last ism() call's distance-field matrix into `out`."""
         _check(lib.iso_copy_field(self.handle, row, _ptr(out)))
+        return out
+
+    def joint_histogram(self, i, j, bins):
+        """Joint histogram of ordered pair (i, j) kept by the last MI_REF32 map."""
+        out = np.zeros((bins, bins), dtype=np.uint32)
+        _check(lib.iso_copy_joint_histogram(self.handle, i, j, _ptr(out)))
         return out
 
     # ---- stages -----------------------------------------------------------
@@ -372,10 +386,11 @@ def select_representatives(ism, ids, isovalues, cnt=16):
     return [(out[i].isovalue, out[i].priority, out[i].id, out[i].map_id) for i in range(k)]
 
 
-# ---- reference-named drop-in functions (device 0) ---------------------------
+# ---- reference-named drop-in functions (the current CUDA device) -------------
 
 def calculate_histogram_h(fields, mins, maxs, bins, sim_size=None, multi=False):
-    """Calls the reference-named entry.  fields: list of 1-D float32 arrays."""
+    """Calls the reference-named entry (the reference's FP32 map, bit for bit).
+    fields: list of 1-D float32 arrays."""
     fields = [np.ascontiguousarray(f, dtype=np.float32) for f in fields]
     nf = len(fields) // 2 if multi else len(fields)
     n = fields[0].size

@@ -211,6 +211,17 @@ def select_representatives(ism, ids, isos, cnt=16):
 
 # ---- the reference's own functions (only where oracle/_ref was built) -------
 
+def reference_root():
+    """Where oracle/build_ref.sh found the reference's sources, or None (the
+    file exists only where they were present when the checkers were built)."""
+    path = os.path.join(os.path.dirname(REF_SO), "reference_root.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        root = f.read().strip()
+    return root if os.path.isdir(root) else None
+
+
 def load_reference():
     """Returns the reference harness library, or None if it was not built."""
     if not os.path.exists(REF_SO):

@@ -30,7 +30,8 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 import oracle  # noqa: E402
 
-REF_TABLES = "/root/reference/isosurfaces_lib/isosurfaces_cuda/src/tables.h"
+_REF_ROOT = oracle.reference_root()
+REF_TABLES = os.path.join(_REF_ROOT, "isosurfaces_lib", "isosurfaces_cuda", "src", "tables.h") if _REF_ROOT else None
 
 
 def bucket_mi(ref):

@@ -10,7 +10,8 @@ import pytest
 import oracle
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
-REF_TABLES = "/root/reference/isosurfaces_lib/isosurfaces_cuda/src/tables.h"
+_REF_ROOT = oracle.reference_root()
+REF_TABLES = os.path.join(_REF_ROOT, "isosurfaces_lib", "isosurfaces_cuda", "src", "tables.h") if _REF_ROOT else None
 
 
 def load(name):
@@ -74,7 +75,7 @@ def test_mc_table_derivation_matches_reference_hash():
     assert hashlib.sha256(derived.tobytes()).hexdigest() == str(g["sha256"])
 
 
-@pytest.mark.skipif(not os.path.exists(REF_TABLES), reason="reference tree not present")
+@pytest.mark.skipif(not REF_TABLES or not os.path.exists(REF_TABLES), reason="reference tree not present")
 def test_mc_table_derivation_matches_reference_text():
     import re
     src = open(REF_TABLES).read()
