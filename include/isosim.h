@@ -118,6 +118,9 @@ ISO_API int64_t iso_ctx_launches(iso_ctx *ctx);
                                                its count and write passes while that table takes at
                                                most this many bytes (default 2^30), else the write
                                                pass counts again; 0 = always count again */
+#define ISO_LIMIT_DEVICE_BYTES 5 /* the context's arena may hold at most this many bytes (0 =
+                                     no cap, the default); a call whose buffers would exceed it
+                                     fails with ISO_ERR_NOMEM and leaves the context usable */
 #define ISO_LIMIT_MI_MODE 4 /* ISO_MI_*: how the mutual information of a pair is computed
                                 (default ISO_MI_FP64; the reference-named entry points use
                                 ISO_MI_REF32) */
@@ -200,7 +203,7 @@ ISO_API int iso_surface_points(iso_ctx *ctx, const float *volume, int X, int Y, 
                                iso_surface_stats *stats_out);
 
 /* Distance field of one point set given in normalised coordinates (p / max(X,Y,Z),
- * isosurfaces_cuda/funcs.cpp:209-233): out[i] = sqrt(min_p |s_i - p|^2) over the
+ * isosurfaces_cuda/funcs.cpp:150-175): out[i] = sqrt(min_p |s_i - p|^2) over the
  * sample grid of isosurfaces_cuda/src/BVH.cu:393-406 (a single point gives the
  * squared distance, BVH.cu:604-611).  points: P xyz triples (host or device);
  * out: (X/ds)(Y/ds)(Z/ds) floats (host or device). */

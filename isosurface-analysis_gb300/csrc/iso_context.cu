@@ -105,6 +105,10 @@ extern "C" int iso_ctx_set_limit(iso_ctx *ctx, int which, int64_t value)
         if (value < 0) return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: byte limit must be >= 0");
         ctx->surf_block_count_bytes = value;
         return ISO_OK;
+    case ISO_LIMIT_DEVICE_BYTES:
+        if (value < 0) return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: byte cap must be >= 0");
+        ctx->device_bytes_cap = value;
+        return ISO_OK;
     case ISO_LIMIT_MI_MODE:
         if (value != ISO_MI_FP64 && value != ISO_MI_REF32)
             return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: unknown MI mode %lld", (long long)value);
@@ -131,6 +135,15 @@ int iso_buf(iso_ctx *ctx, IsoBuf b, size_t bytes, void **out)
 {
     if (bytes == 0) bytes = 256;
     if (ctx->cap[b] < bytes) {
+        size_t want = bytes + bytes / 8;
+        want = (want + 4095) & ~size_t(4095);
+        if (ctx->device_bytes_cap > 0) {
+            size_t held = 0;
+            for (int k = 0; k < BUF_COUNT_; ++k) held += ctx->cap[k];
+            if (held - ctx->cap[b] + want > (size_t)ctx->device_bytes_cap)
+                return iso_fail(ISO_ERR_NOMEM, "device allocation of %zu bytes would exceed the context's cap of %lld "
+                                "bytes (%zu held)", want, (long long)ctx->device_bytes_cap, held);
+        }
         if (ctx->buf[b]) {
             // the old buffer may still be read by queued work on this stream
             ISO_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -138,8 +151,6 @@ int iso_buf(iso_ctx *ctx, IsoBuf b, size_t bytes, void **out)
             ctx->buf[b] = nullptr;
             ctx->cap[b] = 0;
         }
-        size_t want = bytes + bytes / 8;
-        want = (want + 4095) & ~size_t(4095);
         void *p = nullptr;
         cudaError_t e = cudaMalloc(&p, want);
         if (e != cudaSuccess) {

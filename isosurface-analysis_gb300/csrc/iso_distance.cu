@@ -4,7 +4,7 @@
 // (isosurfaces_cuda/src/BVH.cu:108-383, 393-706, 814-875).  The sample point of
 // DF index idx (z fastest over the (X/ds, Y/ds, Z/ds) grid) is
 // ((x*ds + ds/2)/X, (y*ds + ds/2)/Y, (z*ds + ds/2)/Z) (BVH.cu:393-406); surface
-// points are normalised by max(X,Y,Z) (funcs.cpp:209-233).  The field value is
+// points are normalised by max(X,Y,Z) (funcs.cpp:150-175).  The field value is
 // sqrt(min over points of the canonical squared distance); a one-point surface
 // stores the squared distance, as the reference does (BVH.cu:604-611).
 //

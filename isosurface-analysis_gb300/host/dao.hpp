@@ -38,6 +38,7 @@ struct EngineOptions {
     int surface = -1;         // -1: the module's default; 0 marching cubes; 1 approximation
     int distance = 1;         // 0 brute force; 1 LBVH
     int representatives = 16; // MULTI_MAP_DF_NUMBER (globals.h:32)
+    int mi = 1;               // "ref32" (1, default): the reference's own FP32 map; "fp64" (0)
     std::vector<float> list;  // explicit isovalues (overrides isovalues/uniform)
 
     static EngineOptions from(const Value &parent)
@@ -51,6 +52,11 @@ struct EngineOptions {
         if (v.has("surface")) e.surface = v.at("surface").str() == "mc" ? 0 : 1;
         if (v.has("distance")) e.distance = v.at("distance").str() == "brute" ? 0 : 1;
         if (v.has("representatives")) e.representatives = v.at("representatives").integer();
+        if (v.has("mi")) {
+            const std::string mi = v.at("mi").str();
+            if (mi != "ref32" && mi != "fp64") throw std::runtime_error("engine.mi must be \"ref32\" or \"fp64\"");
+            e.mi = mi == "ref32" ? 1 : 0;
+        }
         if (v.has("isovalueList"))
             for (auto &x : v.at("isovalueList").items()) e.list.push_back((float)x.num());
         return e;
@@ -121,6 +127,7 @@ struct MultiVarConfig {  // DAO/hdr/MultiVarConfig.h
     std::string dataRoot;
     int dfDownscale = 1;
     int bins = 128;
+    int mi = 1;  // EngineOptions::mi
 
     static MultiVarConfig from(const Value &v)
     {
@@ -129,7 +136,9 @@ struct MultiVarConfig {  // DAO/hdr/MultiVarConfig.h
         c.timeSteps = ints(v.at("timeSteps"));
         c.dataRoot = v.at("dataRoot").str();
         c.dfDownscale = v.at("dfDownscale").integer();
-        c.bins = EngineOptions::from(v).bins;
+        const EngineOptions e = EngineOptions::from(v);
+        c.bins = e.bins;
+        c.mi = e.mi;
         return c;
     }
 };

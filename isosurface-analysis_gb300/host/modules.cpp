@@ -129,6 +129,8 @@ int run_single(iso_ctx *ctx, const SingleConfig &cfg, bool approximation, const 
     std::vector<int32_t> ids(n);
     int32_t m = 0;
     iso_timing timing{};
+    // map.dat holds the reference's own FP32 map unless the config asks for FP64
+    check(iso_ctx_set_limit(ctx, ISO_LIMIT_MI_MODE, eng.mi ? ISO_MI_REF32 : ISO_MI_FP64), "MI mode");
     check(iso_ism(ctx, img.data(), X, Y, Z, isovalues.data(), n, &o, ism.data(), ids.data(), &m, nullptr, &timing),
           "similarity map");
     ism.resize((size_t)m * m);
@@ -258,6 +260,9 @@ int module_multi(const std::string &json, const RunOptions &opt)
     const std::string prefix = cfg.dataRoot + "-multi-tmp/";
     iso_ctx *ctx = nullptr;
     check(iso_ctx_create(opt.device, &ctx), "context");
+    // the cross maps hold the reference's own FP32 values (its multi mode of
+    // calculate_histogram_h) unless the config asks for FP64
+    check(iso_ctx_set_limit(ctx, ISO_LIMIT_MI_MODE, cfg.mi ? ISO_MI_REF32 : ISO_MI_FP64), "MI mode");
     std::vector<float> a((size_t)R * size), b((size_t)R * size), out((size_t)R * R);
 
     auto load_set = [&](const std::string &var, int t, std::vector<float> &dst) {

@@ -179,12 +179,22 @@ class Context:
     def stream(self):
         return lib.iso_ctx_stream(self.handle)
 
+    @property
+    def device_bytes(self):
+        """Bytes the context's device arena holds."""
+        return lib.iso_ctx_device_bytes(self.handle)
+
     def set_lbvh_group_points(self, points):
         _check(lib.iso_ctx_set_limit(self.handle, 1, int(points)))
 
     def set_hist_segment_values(self, values):
         """Fields longer than `values` use the segment-major histogram schedule (0: never)."""
         _check(lib.iso_ctx_set_limit(self.handle, 2, int(values)))
+
+    def set_device_bytes_cap(self, nbytes):
+        """Largest arena the context may hold (0: no cap); beyond it calls fail
+        with ISO_ERR_NOMEM."""
+        _check(lib.iso_ctx_set_limit(self.handle, 5, int(nbytes)))
 
     def set_mi_mode(self, mode):
         """MI_FP64 (default: accurate, symmetric) or MI_REF32 (the reference's

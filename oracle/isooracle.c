@@ -366,7 +366,7 @@ ORC_API long orc_marching_cubes(const float *img, int X, int Y, int Z, float iso
 /* Distance fields                                                            */
 /* ------------------------------------------------------------------------- */
 
-/* Host normalisation of isosurfaces_cuda/funcs.cpp:209-233: p / max(X,Y,Z). */
+/* Host normalisation of isosurfaces_cuda/funcs.cpp:150-175: p / max(X,Y,Z). */
 ORC_API void orc_normalize_points(const float *pts, long n, int X, int Y, int Z, float *out)
 {
     int dmax = X > Y ? X : Y;

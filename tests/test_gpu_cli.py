@@ -39,6 +39,8 @@ def test_single_module(tmp_path):
     lo, hi = oracle.real_range(vol, -1e9, 1e9)
     isos = oracle.isovalues(vol, lo, hi, 24, uniform=True)
     with isosim.Context(0) as ctx:
+        # map.dat holds the reference's own FP32 map (the module default)
+        ctx.set_mi_mode(isosim.MI_REF32)
         ism, ids, _, _ = ctx.ism(vol.ravel(), dims, isos, surface=isosim.SURFACE_APPROX, bins=32)
     folder = tmp_path / "out" / "V-3"
     got = np.fromfile(folder / "similarityMap-24--approx-scale_1" / "map.dat", np.float32)
@@ -100,8 +102,47 @@ def test_script_then_multi(tmp_path):
                           np.float32) for i in range(16)]
         for i in range(16):
             for j in range(16):
-                joint, _, _ = oracle.pair_histogram(fa[i], fb[j], 32, oracle.field_interval(fa[i]),
-                                                    oracle.field_interval(fb[j]))
-                assert abs(got[i, j] - oracle.mi_f64(joint, F)) < 1e-6
+                joint, cs, rs = oracle.pair_histogram(fa[i], fb[j], 32, oracle.field_interval(fa[i]),
+                                                      oracle.field_interval(fb[j]))
+                # the reference's FP32 MI (device evaluation vs the host restatement)
+                assert abs(got[i, j] - oracle.mi_f32(joint, cs, rs, F)) < 1e-5
     r = subprocess.run([CLI, "check", str(tmp_path / "out" / "meta.json"), "0", "2"], capture_output=True, text=True)
     assert r.returncode == 0 and "0 missing" in r.stdout
+
+
+def test_short_volume_file_is_an_error(tmp_path):
+    """A .dat file with fewer than X*Y*Z floats: the module stops with an
+    error naming the file, and writes no map."""
+    dims = (20, 18, 16)
+    vol = make_volume(2, dims)
+    write_dat(tmp_path / "vol.dat", vol)
+    data = (tmp_path / "vol.dat").read_bytes()
+    (tmp_path / "vol.dat").write_bytes(data[: len(data) - 4 * 17])
+    cfg = {"fileName": str(tmp_path / "vol"), "dimensions": list(dims), "minValue": -1e9, "maxValue": 1e9,
+           "outputFolder": str(tmp_path / "out"), "variableName": "V", "timestep": 0, "jsonFile": "meta.json",
+           "dfDownscale": 1, "engine": {"isovalues": 8, "bins": 32}}
+    (tmp_path / "single.json").write_text(json.dumps(cfg))
+    r = subprocess.run([CLI, "single", str(tmp_path / "single.json")], capture_output=True, text=True)
+    assert r.returncode != 0
+    assert "short read" in r.stderr and "vol.dat" in r.stderr
+    assert not (tmp_path / "out" / "meta.json").exists()
+
+
+def test_allocation_failure_leaves_context_usable():
+    """An allocation the context may not make (its byte cap) fails the call
+    with ISO_ERR_NOMEM; the same context then runs the request normally."""
+    import isosim
+    vol = make_volume(3, (32, 32, 32))
+    import isosim.synth as synth
+    isos = synth.inside_isovalues(vol, 12)
+    with isosim.Context(0) as ref:
+        want, want_ids, _, _ = ref.ism(vol.ravel(), (32, 32, 32), isos, bins=64)
+    with isosim.Context(0) as ctx:
+        ctx.set_device_bytes_cap(1 << 20)
+        with pytest.raises(isosim.IsoError) as e:
+            ctx.ism(vol.ravel(), (32, 32, 32), isos, bins=64)
+        assert e.value.code == isosim.ISO_ERR_NOMEM and "cap" in str(e.value)
+        assert ctx.device_bytes <= 1 << 20
+        ctx.set_device_bytes_cap(0)
+        got, ids, _, _ = ctx.ism(vol.ravel(), (32, 32, 32), isos, bins=64)
+    assert np.array_equal(ids, want_ids) and np.array_equal(got, want)
