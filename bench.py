@@ -161,7 +161,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     vol, isos, bins, name = workload(args.config)
     X, Y, Z = vol.shape
-    method = isosim.DF_LBVH if args.df == "lbvh" else isosim.DF_BRUTE
+    method = {"lbvh": isosim.DF_LBVH, "brute": isosim.DF_BRUTE, "tc": isosim.DF_TC}[args.df]
     ctx = isosim.Context(local)
     if getattr(args, "hist_seg", None) is not None:
         ctx.set_hist_segment_values(args.hist_seg)
@@ -339,7 +339,9 @@ def plain_leg(ctx, vol, isos, sstats, stage, pairs, value, k_surfaces):
     (df_brute_kernel: every sample against every surface point).  The brute
     force over all n surfaces takes minutes at 256^3, so it runs on
     k_surfaces sampled surfaces and is scaled to the whole ISM by
-    (sample, point) pairs -- the brute force's work is exactly F*P per surface."""
+    (sample, point) pairs -- its work is exactly F*P per surface.  The same
+    surfaces also go through the tensor-core brute force (ISO_DF_TC: the
+    contraction on tcgen05 plus exact FP32 candidates), reported beside it."""
     import isosim
     dims = vol.shape
     F = int(np.prod(dims))
@@ -348,23 +350,29 @@ def plain_leg(ctx, vol, isos, sstats, stage, pairs, value, k_surfaces):
     nonempty = np.nonzero(counts)[0]
     pick = nonempty[np.linspace(len(nonempty) // 4, 3 * len(nonempty) // 4, k_surfaces).astype(int)]
     pts, _ = ctx.surface_points(vol.ravel(), dims, isos[pick], surface=isosim.SURFACE_MC, frame=isosim.FRAME_REF)
-    work, secs = 0.0, 0.0
-    for p in pts:
-        pn = (p / np.float32(max(dims))).astype(np.float32)
-        ctx.distance_field(pn[:64], dims, method=isosim.DF_BRUTE)  # warm-up
-        t0 = time.perf_counter()
-        ctx.distance_field(pn, dims, method=isosim.DF_BRUTE)
-        secs += time.perf_counter() - t0
-        work += float(F) * len(p)
-    rate = work / secs
-    df_s = float(F) * float(counts.sum()) / rate
-    t_ism = (stage[0] + stage[2]) / 1e3 + df_s
-    plain = pairs / t_ism
-    return {"value": round(plain, 2), "unit": "pairs/s", "extrapolated": True,
-            "distance": "brute-force FP32 (df_brute_kernel)", "seconds_per_ism": round(t_ism, 2),
-            "sample": "%d of %d surfaces (%d points) timed by brute force, %.3g (sample, point) pairs/s, scaled to "
-                      "all %d surface points; surfaces and histograms as measured above"
-                      % (len(pts), len(nonempty), int(sum(len(p) for p in pts)), rate, int(counts.sum())),
+    out = {}
+    for key, method in (("brute_fp32", isosim.DF_BRUTE), ("tensor_core", isosim.DF_TC)):
+        work, secs = 0.0, 0.0
+        for p in pts:
+            pn = (p / np.float32(max(dims))).astype(np.float32)
+            ctx.distance_field(pn[:300], dims, method=method)  # warm-up
+            t0 = time.perf_counter()
+            ctx.distance_field(pn, dims, method=method)
+            secs += time.perf_counter() - t0
+            work += float(F) * len(p)
+        rate = work / secs
+        df_s = float(F) * float(counts.sum()) / rate
+        t_ism = (stage[0] + stage[2]) / 1e3 + df_s
+        out[key] = {"value": round(pairs / t_ism, 2), "unit": "pairs/s", "seconds_per_ism": round(t_ism, 2),
+                    "sample_point_pairs_per_s": float("%.4g" % rate)}
+    plain = out["brute_fp32"]["value"]
+    return {"value": plain, "unit": "pairs/s", "extrapolated": True,
+            "distance": "brute-force FP32 (df_brute_kernel)", "seconds_per_ism": out["brute_fp32"]["seconds_per_ism"],
+            "sample": "%d of %d surfaces (%d points) timed by brute force on the CUDA cores and on the tensor cores, "
+                      "scaled to all %d surface points by (sample, point) pairs; surfaces and histograms as measured "
+                      "above" % (len(pts), len(nonempty), int(sum(len(p) for p in pts)), int(counts.sum())),
+            "brute_sample_point_pairs_per_s": out["brute_fp32"]["sample_point_pairs_per_s"],
+            "tensor_core": out["tensor_core"],
             "batched_over_plain": round(value / plain, 1)}
 
 
@@ -722,7 +730,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", type=int, default=3, choices=[1, 2, 3])
-    ap.add_argument("--df", default="lbvh", choices=["lbvh", "brute"])
+    ap.add_argument("--df", default="lbvh", choices=["lbvh", "brute", "tc"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--hist-seg", type=int, default=None,
                     help="segment length of the segment-major histogram schedule (0: fused kernel only)")

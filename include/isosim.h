@@ -56,6 +56,10 @@ extern "C" {
 /* distance-field method; all give bit-identical fields */
 #define ISO_DF_BRUTE 0 /* every sample against every surface point, FP32 */
 #define ISO_DF_LBVH 1  /* linear BVH (Morton codes, radix sort, Karras hierarchy, stack query) */
+#define ISO_DF_TC 2    /* every sample against every point as a tensor-core contraction
+                          |s-p|^2 = |s|^2 + |p|^2 - 2 s.p (split-f16 operands, FP32 accumulation)
+                          that selects candidates; each candidate's distance is then
+                          computed exactly in FP32 */
 
 /* marching-cubes result flags (iso_surface_stats.flags) */
 #define ISO_MC_REF_DROPPED 1 /* more than V-3 triangle vertices: the reference drops triangles here */

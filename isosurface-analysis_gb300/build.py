@@ -25,6 +25,7 @@ SOURCES = [
     "iso_context.cu",
     "iso_surface.cu",
     "iso_distance.cu",
+    "iso_distance_tc.cu",
     "iso_histogram.cu",
     "iso_mi_ref32.cu",
     "iso_pipeline.cu",
@@ -32,7 +33,8 @@ SOURCES = [
     "iso_multi.cu",
     "iso_reps.cpp",
 ]
-HEADERS = [os.path.join(CSRC, "iso_internal.cuh"), os.path.join(ROOT, "include", "isosim.h")]
+HEADERS = [os.path.join(CSRC, "iso_internal.cuh"), os.path.join(CSRC, "iso_tc.cuh"),
+           os.path.join(ROOT, "include", "isosim.h")]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = [

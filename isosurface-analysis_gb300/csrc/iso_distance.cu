@@ -35,28 +35,11 @@ constexpr int QUERY_THREADS = 128;
 constexpr int STACK_DEPTH = 64;
 constexpr float INIT_BOUND = 100000.0f;  // the reference's initial upper bound (BVH.cu:639)
 
-struct SampleGrid {
-    int X, Y, Z, ds;
-    int64_t Y10, Z10, F;
-};
+using SampleGrid = IsoSampleGrid;
+using Segments = IsoSegments;
 
-__device__ __forceinline__ float3 sample_point(const SampleGrid &g, int64_t idx)
-{
-    int64_t z = idx % g.Z10, y = (idx / g.Z10) % g.Y10, x = idx / (g.Y10 * g.Z10);
-    float3 s;
-    s.x = __fdiv_rn((float)(x * g.ds + g.ds / 2), (float)g.X);
-    s.y = __fdiv_rn((float)(y * g.ds + g.ds / 2), (float)g.Y);
-    s.z = __fdiv_rn((float)(z * g.ds + g.ds / 2), (float)g.Z);
-    return s;
-}
-
-__device__ __forceinline__ float finish(float best, int64_t P) { return P == 1 ? best : __fsqrt_rn(best); }
-
-struct Segments {
-    const float4 *points;   // normalised points (w unused)
-    const int64_t *offset;  // per segment: first point
-    const int64_t *count;   // per segment: number of points
-};
+__device__ __forceinline__ float3 sample_point(const SampleGrid &g, int64_t idx) { return iso_sample_point(g, idx); }
+__device__ __forceinline__ float finish(float best, int64_t P) { return iso_df_finish(best, P); }
 
 __global__ void __launch_bounds__(BRUTE_THREADS) df_brute_kernel(Segments sg, SampleGrid g, float *fields,
                                                                    int64_t stride, int seg_base)
@@ -713,6 +696,8 @@ int iso_run_distance(iso_ctx *ctx, int X, int Y, int Z, int ds, int method, cons
                                                                              field_stride, base);
             ISO_LAUNCHED(ctx);
         }
+    } else if (method == ISO_DF_TC) {
+        ISO_TRY(iso_run_distance_tc(ctx, g, sg, h_seg_count, m, fields, field_stride));
     } else if (method == ISO_DF_LBVH) {
         // surfaces are processed in groups of at most ctx->lbvh_group_points
         // points (one surface may exceed it alone), which bounds the LBVH

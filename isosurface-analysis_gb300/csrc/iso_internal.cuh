@@ -163,6 +163,43 @@ __device__ __forceinline__ int iso_bucket(float v, float mn, float step, int bin
     return b < 0 ? 0 : b;
 }
 
+// Distance-field sample grid: the sample of DF index idx (z fastest over the
+// (X/ds, Y/ds, Z/ds) grid) is ((x*ds + ds/2)/X, (y*ds + ds/2)/Y, (z*ds + ds/2)/Z)
+// (isosurfaces_cuda/src/BVH.cu:393-406).
+struct IsoSampleGrid {
+    int X, Y, Z, ds;
+    int64_t Y10, Z10, F;
+};
+
+__device__ __forceinline__ float3 iso_sample_point(const IsoSampleGrid &g, int64_t idx)
+{
+    int64_t z = idx % g.Z10, y = (idx / g.Z10) % g.Y10, x = idx / (g.Y10 * g.Z10);
+    float3 s;
+    s.x = __fdiv_rn((float)(x * g.ds + g.ds / 2), (float)g.X);
+    s.y = __fdiv_rn((float)(y * g.ds + g.ds / 2), (float)g.Y);
+    s.z = __fdiv_rn((float)(z * g.ds + g.ds / 2), (float)g.Z);
+    return s;
+}
+
+// Field value from the minimum canonical squared distance: its square root,
+// except that a one-point surface keeps the squared distance (BVH.cu:604-611).
+__device__ __forceinline__ float iso_df_finish(float best, int64_t P) { return P == 1 ? best : __fsqrt_rn(best); }
+
+// The reference's initial upper bound of a nearest-point search (BVH.cu:639).
+constexpr float ISO_DF_INIT_BOUND = 100000.0f;
+
+// Point sets of a distance-field launch.
+struct IsoSegments {
+    const float4 *points;   // normalised points (w unused)
+    const int64_t *offset;  // per segment: first point
+    const int64_t *count;   // per segment: number of points
+};
+
+// Tensor-core distance fields (csrc/iso_distance_tc.cu): segment q's field
+// into fields + q*stride, for q < m.
+int iso_run_distance_tc(iso_ctx *ctx, const IsoSampleGrid &g, const IsoSegments &sg, const int64_t *h_seg_count, int m,
+                        float *fields, int64_t stride);
+
 // Host-side launch helpers implemented per stage.
 int iso_run_surfaces(iso_ctx *ctx, const float *d_vol, int X, int Y, int Z, const float *h_iso, int n,
                      int surface, int frame, int64_t *h_counts, int64_t *h_offsets,

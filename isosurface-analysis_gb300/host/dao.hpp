@@ -163,12 +163,24 @@ struct SimilarityMapInformation {  // DAO/hdr/SimilarityMapInformation.h
     std::string filename;
 };
 
+// A timestep (TSM) or variable (VSM) similarity matrix built from cross maps.
+// No counterpart in the reference's ledger schema: written under the
+// additional key "aggregateMaps", and only when there are some, so that
+// ledgers without them keep the reference's keys exactly.
+struct AggregateMapInformation {
+    std::string kind;  // "TSM" (one variable over timesteps) or "VSM" (one timestep over variables)
+    int variable = -1; // TSM: variable index; VSM: -1
+    int timestep = -1; // VSM: timestep; TSM: -1
+    std::string filename;
+};
+
 struct RunInformation {  // DAO/hdr/RunInformation.h, src/RunInformation.cpp
     std::vector<int> dimensions;
     std::vector<std::string> variables;
     int dfDownscale = 1;
     std::vector<VolumeInformation> volumes;
     std::vector<SimilarityMapInformation> similarityMaps;
+    std::vector<AggregateMapInformation> aggregateMaps;
 
     int variable_index(const std::string &name)
     {
@@ -197,6 +209,17 @@ struct RunInformation {  // DAO/hdr/RunInformation.h, src/RunInformation.cpp
         m.t2 = t2;
         m.filename = file;
         similarityMaps.push_back(m);
+    }
+
+    // Replaces any earlier matrix of the same kind, variable and timestep.
+    void setAggregateMap(const std::string &kind, int variable, int timestep, const std::string &file)
+    {
+        for (auto &a : aggregateMaps)
+            if (a.kind == kind && a.variable == variable && a.timestep == timestep) {
+                a.filename = file;
+                return;
+            }
+        aggregateMaps.push_back({kind, variable, timestep, file});
     }
 
     static RunInformation from(const Value &v)
@@ -232,6 +255,10 @@ struct RunInformation {  // DAO/hdr/RunInformation.h, src/RunInformation.cpp
             m.filename = x.at("filename").str();
             r.similarityMaps.push_back(m);
         }
+        if (v.has("aggregateMaps"))
+            for (auto &x : v.at("aggregateMaps").items())
+                r.aggregateMaps.push_back({x.at("kind").str(), x.at("variable").integer(), x.at("timestep").integer(),
+                                           x.at("filename").str()});
         return r;
     }
 
@@ -276,6 +303,18 @@ struct RunInformation {  // DAO/hdr/RunInformation.h, src/RunInformation.cpp
             maps.push(x);
         }
         o.set("similarityMaps", maps);
+        if (!aggregateMaps.empty()) {
+            Value agg = Value::array();
+            for (auto &a : aggregateMaps) {
+                Value x = Value::object();
+                x.set("kind", Value(a.kind));
+                x.set("variable", Value(a.variable));
+                x.set("timestep", Value(a.timestep));
+                x.set("filename", Value(a.filename));
+                agg.push(x);
+            }
+            o.set("aggregateMaps", agg);
+        }
         return o;
     }
 };

@@ -15,7 +15,9 @@ static void usage()
             "usage: isosim <module> <args>\n"
             "  single <SingleConfig.json>        one volume (voxel approximation)\n"
             "  script <ScriptingInput.json>      entries x variables x timesteps (marching cubes)\n"
-            "  multi  <MultiVarConfig.json>      16x16 cross maps between representative fields\n"
+            "  multi  <MultiVarConfig.json>      16x16 cross maps between representative fields,\n"
+            "                                    timestep and variable similarity matrices\n"
+            "  distance <SingleConfig.json>      equalise 16 distances between 17 isovalues\n"
             "  stitch <host.json> <part.json>... merge run ledgers into stitched.json\n"
             "  check  <meta.json> <ts1> <ts2>    list missing cross maps\n"
             "options (before the module): --device N, --quiet\n");
@@ -38,6 +40,7 @@ int main(int argc, char **argv)
         if (module == "single" && rest.size() == 1) return isomod::module_single(rest[0], opt);
         if (module == "script" && rest.size() == 1) return isomod::module_script(rest[0], opt);
         if (module == "multi" && rest.size() == 1) return isomod::module_multi(rest[0], opt);
+        if (module == "distance" && rest.size() == 1) return isomod::module_distance(rest[0], opt);
         if (module == "stitch") return isomod::module_stitch(rest, opt);
         if (module == "check" && rest.size() == 3)
             return isomod::module_check(rest[0], atoi(rest[1].c_str()), atoi(rest[2].c_str()), opt);

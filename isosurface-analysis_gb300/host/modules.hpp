@@ -19,6 +19,7 @@ int run_single(iso_ctx *ctx, const isodao::SingleConfig &cfg, bool approximation
 int module_single(const std::string &json, const RunOptions &opt);
 int module_script(const std::string &json, const RunOptions &opt);
 int module_multi(const std::string &json, const RunOptions &opt);
+int module_distance(const std::string &json, const RunOptions &opt);
 int module_stitch(const std::vector<std::string> &files, const RunOptions &opt);
 int module_check(const std::string &json, int ts1, int ts2, const RunOptions &opt);
 

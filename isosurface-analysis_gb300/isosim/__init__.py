@@ -26,6 +26,7 @@ FRAME_REF = 0
 FRAME_CANON = 1
 DF_BRUTE = 0
 DF_LBVH = 1
+DF_TC = 2
 MI_FP64 = 0
 MI_REF32 = 1
 MC_REF_DROPPED = 1

@@ -108,6 +108,24 @@ def test_script_then_multi(tmp_path):
                 assert abs(got[i, j] - oracle.mi_f32(joint, cs, rs, F)) < 1e-5
     r = subprocess.run([CLI, "check", str(tmp_path / "out" / "meta.json"), "0", "2"], capture_output=True, text=True)
     assert r.returncode == 0 and "0 missing" in r.stdout
+    # timestep and variable similarity matrices over those cross maps
+    agg = {(a["kind"], a["variable"], a["timestep"]): a["filename"] for a in meta["aggregateMaps"]}
+    assert set(agg) == {("TSM", 0, -1), ("TSM", 1, -1), ("VSM", -1, 0), ("VSM", -1, 1)}
+    maps = {(a, t1, b, t2): np.fromfile(f, np.float32).reshape(16, 16) for a, t1, b, t2, f in cross}
+
+    def summary(m):
+        return float(m.mean()), 0.5 * (float(m.max(axis=1).mean()) + float(m.max(axis=0).mean()))
+
+    tsm = json.loads(open(agg[("TSM", names.index("A"), -1)]).read())
+    assert tsm["variable"] == "A" and tsm["timesteps"] == steps
+    mean, best = summary(maps[("A", 0, "A", 1)])
+    assert abs(tsm["mean"][0][1] - mean) < 1e-5 and abs(tsm["bestMatch"][0][1] - best) < 1e-5
+    assert abs(tsm["bestMatch"][1][0] - best) < 1e-5 and tsm["mean"][0][0] == 1.0
+    vsm = json.loads(open(agg[("VSM", -1, 1)]).read())
+    assert vsm["variables"] == names
+    mean, best = summary(maps[("A", 1, "B", 1)])
+    ia, ib = names.index("A"), names.index("B")
+    assert abs(vsm["mean"][ia][ib] - mean) < 1e-5 and abs(vsm["bestMatch"][ia][ib] - best) < 1e-5
 
 
 def test_short_volume_file_is_an_error(tmp_path):
