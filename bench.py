@@ -175,6 +175,17 @@ def run_ours(args):
         return ctx.ism(vol_arg, (X, Y, Z), isos, surface=isosim.SURFACE_MC, frame=isosim.FRAME_REF,
                        df_method=method, bins=bins, out=out)
 
+    # the engine's autotuner picks the launch shapes for this workload (cached
+    # on disk; trials run before the warm-up, outside every timed region)
+    tuning = None
+    if not args.no_tune and args.hist_seg is None:
+        import tempfile
+        t = ctx.autotune(d_vol, (X, Y, Z), isos, surface=isosim.SURFACE_MC, frame=isosim.FRAME_REF,
+                         df_method=method, bins=bins,
+                         cache_path=os.path.join(tempfile.gettempdir(), "isosim_tune_cache.txt"))
+        tuning = {"hist_segment_values": int(t.hist_segment_values), "lbvh_group_points": int(t.lbvh_group_points),
+                  "query_run": int(t.query_run) or "by volume size", "from_cache": bool(t.from_cache),
+                  "trials": int(t.trials), "default_ms": round(t.default_ms, 2), "tuned_ms": round(t.tuned_ms, 2)}
     for _ in range(args.warmup):
         _, ids, sstats, timing = step(d_vol, ism_dev)
     m = len(ids)
@@ -229,7 +240,8 @@ def run_ours(args):
     # bytes = each distance field read once + each joint histogram written once
     F = X * Y * Z
     hist_bytes = 4.0 * F * m + 4.0 * bins * bins * pairs
-    seg_values = 2097152 if args.hist_seg is None else args.hist_seg  # the engine's default
+    seg_values = (tuning["hist_segment_values"] if tuning else
+                  (2097152 if args.hist_seg is None else args.hist_seg))  # the engine's default
     hist_s = stage[2] / 1e3
     peak, peak_kind = load_peaks()
     achieved = hist_bytes / hist_s / 1e9
@@ -289,6 +301,7 @@ def run_ours(args):
         "e2e": {"value": round(world * pairs / (e2e_ms / 1e3), 2), "unit": "pairs/s",
                 "h2d_bytes_per_step": int(F * 4 + n * 4), "d2h_bytes_per_step": int(m * m * 4 + m * 4)},
         "gpu_launches": int(launches),
+        "tuning": tuning,
         "roofline": roofline,
         "clocks": clocks,
     }
@@ -740,6 +753,7 @@ def main():
     ap.add_argument("--ref-scale", type=float, default=0.5,
                     help="sample size of each reference-arm step (see cpu_baseline)")
     ap.add_argument("--no-plain", action="store_true", help="skip the brute-force plain-path leg")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes (no autotuner)")
     ap.add_argument("--plain-surfaces", type=int, default=2)
     ap.add_argument("--serving-requests", type=int, default=24,
                     help="requests of the serving leg in the default line (0: none)")

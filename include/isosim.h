@@ -125,6 +125,9 @@ ISO_API int64_t iso_ctx_launches(iso_ctx *ctx);
 #define ISO_LIMIT_DEVICE_BYTES 5 /* the context's arena may hold at most this many bytes (0 =
                                      no cap, the default); a call whose buffers would exceed it
                                      fails with ISO_ERR_NOMEM and leaves the context usable */
+#define ISO_LIMIT_QUERY_RUN 6 /* LBVH query: samples each lane sweeps along x, 8, 16, 32 or 64
+                                  (0 = by volume size, the default: 64 from 128 samples along x,
+                                  else 8); results are identical for every value */
 #define ISO_LIMIT_MI_MODE 4 /* ISO_MI_*: how the mutual information of a pair is computed
                                 (default ISO_MI_FP64; the reference-named entry points use
                                 ISO_MI_REF32) */
@@ -249,6 +252,29 @@ ISO_API int iso_transpose_xfastest(iso_ctx *ctx, const float *src, int X, int Y,
  * (host or device, (X/ds)(Y/ds)(Z/ds) floats) -- the representative
  * fields the single module writes as distancefield-<k>.df. */
 ISO_API int iso_copy_field(iso_ctx *ctx, int row, float *out);
+
+/* Autotuner: times the whole pipeline on this workload under candidate launch
+ * shapes -- ISO_LIMIT_QUERY_RUN and ISO_LIMIT_LBVH_GROUP_POINTS for the
+ * distance stage, ISO_LIMIT_HIST_SEGMENT_VALUES for the histogram stage --
+ * each judged by the time of its own stage, and applies the best set to the
+ * context (kept only if the whole pipeline is at least as fast as with the
+ * context's previous settings).  Results do not depend on these settings.
+ * cache_path (may be NULL): a text file of earlier choices; a hit applies the
+ * cached set without trials, a miss appends the new choice.  Replaces the
+ * reference's fixed launch shapes (isosurfaces_cuda/src/JointHistogram.cu:
+ * 362-364, BVH.cu:667-673). */
+typedef struct iso_tuning {
+    int64_t hist_segment_values; /* chosen ISO_LIMIT_HIST_SEGMENT_VALUES */
+    int64_t lbvh_group_points;   /* chosen ISO_LIMIT_LBVH_GROUP_POINTS */
+    int32_t query_run;           /* chosen ISO_LIMIT_QUERY_RUN (0 = by volume size) */
+    int32_t from_cache;          /* 1: read from cache_path, no trials run */
+    float default_ms;            /* pipeline time with the previous settings */
+    float tuned_ms;              /* pipeline time with the chosen settings */
+    int32_t trials;              /* pipeline runs timed */
+    int32_t reserved;
+} iso_tuning;
+ISO_API int iso_autotune(iso_ctx *ctx, const float *volume, int X, int Y, int Z, const float *isovalues, int n,
+                         const iso_opts *opts, const char *cache_path, iso_tuning *out);
 
 /* Copies the joint histogram of ordered pair (i, j) (row = bucket of field i)
  * kept by the context's last ISO_MI_REF32 similarity run (iso_ism,

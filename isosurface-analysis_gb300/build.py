@@ -32,6 +32,7 @@ SOURCES = [
     "iso_server.cu",
     "iso_multi.cu",
     "iso_reps.cpp",
+    "iso_tune.cpp",
 ]
 HEADERS = [os.path.join(CSRC, "iso_internal.cuh"), os.path.join(CSRC, "iso_tc.cuh"),
            os.path.join(ROOT, "include", "isosim.h")]

@@ -109,6 +109,11 @@ extern "C" int iso_ctx_set_limit(iso_ctx *ctx, int which, int64_t value)
         if (value < 0) return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: byte cap must be >= 0");
         ctx->device_bytes_cap = value;
         return ISO_OK;
+    case ISO_LIMIT_QUERY_RUN:
+        if (value != 0 && value != 8 && value != 16 && value != 32 && value != 64)
+            return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: query run must be 0, 8, 16, 32 or 64");
+        ctx->query_run = (int)value;
+        return ISO_OK;
     case ISO_LIMIT_MI_MODE:
         if (value != ISO_MI_FP64 && value != ISO_MI_REF32)
             return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: unknown MI mode %lld", (long long)value);

@@ -635,15 +635,18 @@ static int lbvh_group(iso_ctx *ctx, const SampleGrid &g, Segments sg, const int6
         bb.nodes = b.nodes - base;
         const int64_t X10 = g.F / (g.Y10 * g.Z10);
         const int64_t cols = ((g.Y10 + PATCH_Y * WARPS_Y - 1) / (PATCH_Y * WARPS_Y)) * ((g.Z10 + PATCH_Z - 1) / PATCH_Z);
-        const bool long_runs = X10 >= 128;
-        const int run = long_runs ? RUN_X_LONG : RUN_X_SHORT;
+        // samples per lane along x: the context's choice (autotuner), else
+        // 64 for volumes of 128 and more along x, 8 below
+        const int run = ctx->query_run > 0 ? ctx->query_run : (X10 >= 128 ? RUN_X_LONG : RUN_X_SHORT);
         const int64_t bricks = ((X10 + run - 1) / run) * cols;
-        if (long_runs)
-            bvh_query_kernel<RUN_X_LONG, QUERY_GROUP><<<dim3((unsigned)bricks, cnt), QUERY_THREADS, 0, ctx->stream>>>(
-                bb, g, fields + (size_t)base * field_stride, field_stride);
-        else
-            bvh_query_kernel<RUN_X_SHORT, QUERY_GROUP><<<dim3((unsigned)bricks, cnt), QUERY_THREADS, 0, ctx->stream>>>(
-                bb, g, fields + (size_t)base * field_stride, field_stride);
+        const dim3 grid((unsigned)bricks, cnt);
+        float *out = fields + (size_t)base * field_stride;
+        switch (run) {
+        case 8: bvh_query_kernel<8, QUERY_GROUP><<<grid, QUERY_THREADS, 0, ctx->stream>>>(bb, g, out, field_stride); break;
+        case 16: bvh_query_kernel<16, QUERY_GROUP><<<grid, QUERY_THREADS, 0, ctx->stream>>>(bb, g, out, field_stride); break;
+        case 32: bvh_query_kernel<32, QUERY_GROUP><<<grid, QUERY_THREADS, 0, ctx->stream>>>(bb, g, out, field_stride); break;
+        default: bvh_query_kernel<64, QUERY_GROUP><<<grid, QUERY_THREADS, 0, ctx->stream>>>(bb, g, out, field_stride); break;
+        }
         ISO_LAUNCHED(ctx);
     }
     int err = 0;

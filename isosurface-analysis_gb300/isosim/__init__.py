@@ -57,6 +57,12 @@ class Timing(C.Structure):
                 ("total_ms", C.c_float)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("hist_segment_values", C.c_int64), ("lbvh_group_points", C.c_int64), ("query_run", C.c_int32),
+                ("from_cache", C.c_int32), ("default_ms", C.c_float), ("tuned_ms", C.c_float),
+                ("trials", C.c_int32), ("reserved", C.c_int32)]
+
+
 class Request(C.Structure):
     _fields_ = [("volume", C.c_void_p), ("X", C.c_int), ("Y", C.c_int), ("Z", C.c_int),
                 ("isovalues", C.c_void_p), ("n", C.c_int), ("opts", Opts), ("ism_out", C.c_void_p),
@@ -104,6 +110,8 @@ def _load():
         "iso_transpose_xfastest": (C.c_int, [P, P, C.c_int, C.c_int, C.c_int, P]),
         "iso_copy_field": (C.c_int, [P, C.c_int, P]),
         "iso_copy_joint_histogram": (C.c_int, [P, C.c_int, C.c_int, P]),
+        "iso_autotune": (C.c_int, [P, P, C.c_int, C.c_int, C.c_int, P, C.c_int, C.POINTER(Opts), C.c_char_p,
+                                   C.POINTER(Tuning)]),
         "iso_server_create": (C.c_int, [C.c_int, C.c_int, C.c_size_t, C.POINTER(P)]),
         "iso_server_submit": (C.c_int, [P, C.POINTER(Request), C.POINTER(C.c_int64)]),
         "iso_server_wait": (C.c_int, [P, C.c_int64, C.POINTER(RequestResult)]),
@@ -277,6 +285,23 @@ class Context:
         """Row `row` of the last ism() call's distance-field matrix into `out`."""
         _check(lib.iso_copy_field(self.handle, row, _ptr(out)))
         return out
+
+    def autotune(self, volume, dims, isovalues, surface=SURFACE_MC, frame=FRAME_REF, df_method=DF_LBVH,
+                 downscale=1, bins=128, cache_path=None):
+        """Chooses and applies the fastest launch shapes for this workload
+        (see iso_autotune); returns the Tuning record."""
+        X, Y, Z = dims
+        iso = np.ascontiguousarray(isovalues, dtype=np.float32)
+        vol = _f32(volume)
+        opts = Opts(surface, frame, df_method, downscale, bins)
+        t = Tuning()
+        _check(lib.iso_autotune(self.handle, _ptr(vol), X, Y, Z, _ptr(iso), iso.size, C.byref(opts),
+                                cache_path.encode() if cache_path else None, C.byref(t)))
+        return t
+
+    def set_query_run(self, run):
+        """LBVH query samples per lane along x (0: by volume size)."""
+        _check(lib.iso_ctx_set_limit(self.handle, 6, int(run)))
 
     def joint_histogram(self, i, j, bins):
         """Joint histogram of ordered pair (i, j) kept by the last MI_REF32 map."""
