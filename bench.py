@@ -488,7 +488,7 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def serving_stats(requests, rate, slots, budget_gb):
+def serving_stats(requests, rate, slots, budget_gb, max_wait_ms=2000.0):
     """Poisson stream of ISM requests through the serving loop (continuous
     batching under an HBM budget) and through one-request-at-a-time serving.
     Shapes, isovalue counts and bins are drawn per request (seeded); volumes
@@ -524,8 +524,12 @@ def serving_stats(requests, rate, slots, budget_gb):
             isos = np.array([lo + (i + 1) * (hi - lo) / (n + 1) for i in range(n)], np.float32)
         reqs.append((t, vol, sh, isos, bins))
 
-    def serve(slots):
+    costs = np.array([float(np.prod(sh)) * len(isos) * (len(isos) + 64) for (_, _, sh, isos, _) in reqs])
+    small = costs <= np.median(costs)
+
+    def serve(slots, policy):
         with isosim.Server(0, slots=slots, budget_bytes=int(budget_gb * (1 << 30))) as srv:
+            srv.set_policy(policy, max_wait_ms)
             # warm each worker's arena on a small request
             for _ in range(slots):
                 srv.wait(srv.submit(pool[(shapes[0], "blobs")], shapes[0], reqs[0][3][:16], bins=128))
@@ -536,8 +540,8 @@ def serving_stats(requests, rate, slots, budget_gb):
                 if delay > 0:
                     time.sleep(delay)
                 tickets.append((srv.submit(vol, sh, isos, bins=bins), time.perf_counter()))
-            pairs, lat, failed = 0, [], 0
-            for tk, _ in tickets:
+            pairs, lat, lat_small, failed = 0, [], [], 0
+            for q, (tk, _) in enumerate(tickets):
                 try:
                     ism, ids, res = srv.wait(tk)
                 except isosim.IsoError:
@@ -545,17 +549,22 @@ def serving_stats(requests, rate, slots, budget_gb):
                     continue
                 pairs += len(ids) * (len(ids) - 1) // 2
                 lat.append(res.latency_ms)
+                if small[q]:
+                    lat_small.append(res.latency_ms)
             wall = time.perf_counter() - t0
             st = srv.stats()
         lat = np.array(lat)
         return {"pairs_per_s": round(pairs / wall, 1), "wall_s": round(wall, 2), "pairs": int(pairs), "failed": failed,
                 "p50_ms": round(float(np.percentile(lat, 50)), 1), "p99_ms": round(float(np.percentile(lat, 99)), 1),
+                "small_request_p50_ms": round(float(np.percentile(lat_small, 50)), 1) if lat_small else None,
+                "policy": "shortest first" if policy == isosim.SERVE_SHORTEST_FIRST else "fifo",
                 "peak_admitted_gb": round(st.peak_device_bytes / (1 << 30), 2)}
 
-    batched = serve(slots)
-    plain = serve(1)
+    batched = serve(slots, isosim.SERVE_SHORTEST_FIRST)
+    plain = serve(1, isosim.SERVE_FIFO)
     desc = ("Poisson stream of %d requests at %g req/s; shapes %s; isovalues {16..256}; bins {128,256}; "
-            "%g GB HBM budget; %d slots" % (requests, rate, shapes, budget_gb, slots))
+            "%g GB HBM budget; %d slots; small requests: work estimate at or below the median"
+            % (requests, rate, shapes, budget_gb, slots))
     return batched, plain, desc
 
 

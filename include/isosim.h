@@ -371,6 +371,15 @@ typedef struct iso_server_stats {
  * trimmed to make room; waiting requests go in submission order; a request
  * larger than the budget fails with ISO_ERR_NOMEM). */
 ISO_API int iso_server_create(int device, int slots, size_t hbm_budget_bytes, iso_server **out);
+/* Order in which workers take queued requests.  ISO_SERVE_FIFO (the default):
+ * submission order.  ISO_SERVE_SHORTEST_FIRST: the request with the smallest
+ * work estimate (samples x isovalues x (isovalues + 64)) first, unless the
+ * oldest queued request has waited more than max_wait_ms, which then goes
+ * first; a request smaller than one already running is issued on a
+ * high-priority CUDA stream.  Results are the same under either policy. */
+#define ISO_SERVE_FIFO 0
+#define ISO_SERVE_SHORTEST_FIRST 1
+ISO_API int iso_server_set_policy(iso_server *s, int policy, double max_wait_ms);
 /* Queues a request (the descriptor is copied; the buffers must stay valid
  * until iso_server_wait returns for its ticket). */
 ISO_API int iso_server_submit(iso_server *s, const iso_request *req, int64_t *ticket);

@@ -1,7 +1,10 @@
 // iso_server.cu -- device-resident request loop with continuous batching.
 //
 // A fixed pool of workers, each owning an engine context (its own CUDA stream
-// and device arena), takes ISM requests from a FIFO queue.  Requests run
+// and device arena), takes ISM requests from a queue: first in, first out, or
+// (ISO_SERVE_SHORTEST_FIRST) the smallest work estimate first, with a bound on
+// how long the oldest request may be passed over; a request smaller than one
+// already running then goes to a high-priority stream.  Requests run
 // concurrently on the device as workers free up.  Device memory is admitted
 // against a budget: a request first runs its surface count pass (volume plus
 // small buffers), which fixes its exact need; the worker then waits until
@@ -30,6 +33,7 @@ using Clock = std::chrono::steady_clock;
 
 struct Job {
     iso_request req;
+    double cost = 0;  // work estimate: samples x isovalues x (isovalues + 64)
     int64_t ticket = 0;
     int status = ISO_OK;
     std::string error;
@@ -43,6 +47,9 @@ enum class WState { Idle, Counting, Waiting, Running };
 
 struct Worker {
     iso_ctx *ctx = nullptr;
+    cudaStream_t normal = nullptr;  // the context's own stream
+    cudaStream_t urgent = nullptr;  // a high-priority stream for requests smaller than a running one
+    double cost = 0;                // estimate of the running request (0: none)
     std::thread thread;
     WState state = WState::Idle;
     size_t held = 0;      // arena bytes physically allocated
@@ -55,6 +62,8 @@ struct Worker {
 struct iso_server {
     int device = 0;
     size_t budget = 0;
+    int policy = ISO_SERVE_FIFO;
+    double max_wait_ms = 0;
     std::vector<Worker> workers;
     std::mutex mu;
     std::condition_variable cv_queue, cv_mem, cv_done;
@@ -159,8 +168,26 @@ void worker_loop(iso_server *s, size_t self)
             std::unique_lock<std::mutex> lock(s->mu);
             s->cv_queue.wait(lock, [&] { return s->stop || !s->queue.empty(); });
             if (s->stop && s->queue.empty()) return;
-            job = s->queue.front();
-            s->queue.pop_front();
+            // FIFO, or the smallest estimate first unless the oldest request
+            // has waited longer than max_wait_ms
+            auto pick = s->queue.begin();
+            if (s->policy == ISO_SERVE_SHORTEST_FIRST) {
+                const double waited =
+                    std::chrono::duration<double, std::milli>(Clock::now() - (*pick)->t_submit).count();
+                if (waited <= s->max_wait_ms)
+                    for (auto it = s->queue.begin(); it != s->queue.end(); ++it)
+                        if ((*it)->cost < (*pick)->cost) pick = it;
+            }
+            job = *pick;
+            s->queue.erase(pick);
+            // a request smaller than one already on the device runs on the
+            // high-priority stream, so that its blocks are scheduled first
+            bool urgent = false;
+            if (s->policy == ISO_SERVE_SHORTEST_FIRST)
+                for (size_t w = 0; w < s->workers.size(); ++w)
+                    if (w != self && s->workers[w].cost > job->cost) urgent = true;
+            me.ctx->stream = urgent && me.urgent ? me.urgent : me.normal;
+            me.cost = job->cost;
             me.state = WState::Counting;
             me.ticket = job->ticket;
             job->t_start = Clock::now();
@@ -181,6 +208,8 @@ void worker_loop(iso_server *s, size_t self)
             if (r.m_out) *r.m_out = job->m;
             me.held = iso_ctx_device_bytes(me.ctx);
             me.reserved = 0;
+            me.cost = 0;
+            me.ctx->stream = me.normal;
             me.state = WState::Idle;
             me.ticket = -1;
             if (rc == ISO_OK) {
@@ -214,8 +243,30 @@ extern "C" int iso_server_create(int device, int slots, size_t hbm_budget_bytes,
             return rc;
         }
     }
+    int lo = 0, hi = 0;
+    cudaSetDevice(device);
+    if (cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess) cudaGetLastError();
+    for (int w = 0; w < slots; ++w) {
+        Worker &k = s->workers[w];
+        k.normal = k.ctx->stream;
+        if (cudaStreamCreateWithPriority(&k.urgent, cudaStreamNonBlocking, hi) != cudaSuccess) {
+            cudaGetLastError();
+            k.urgent = nullptr;
+        }
+    }
     for (int w = 0; w < slots; ++w) s->workers[w].thread = std::thread(worker_loop, s, (size_t)w);
     *out = s;
+    return ISO_OK;
+}
+
+extern "C" int iso_server_set_policy(iso_server *s, int policy, double max_wait_ms)
+{
+    iso_clear_error();
+    if (!s || (policy != ISO_SERVE_FIFO && policy != ISO_SERVE_SHORTEST_FIRST) || !(max_wait_ms >= 0))
+        return iso_fail(ISO_ERR_ARG, "iso_server_set_policy: bad argument");
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->policy = policy;
+    s->max_wait_ms = max_wait_ms;
     return ISO_OK;
 }
 
@@ -226,6 +277,11 @@ extern "C" int iso_server_submit(iso_server *s, const iso_request *req, int64_t 
         return iso_fail(ISO_ERR_ARG, "iso_server_submit: bad argument");
     Job *job = new Job();
     job->req = *req;
+    {
+        const double ds = req->opts.df_downscale > 0 ? req->opts.df_downscale : 1;
+        const double F = (double)req->X * req->Y * req->Z / (ds * ds * ds);
+        job->cost = F * req->n * (req->n + 64.0);
+    }
     job->t_submit = Clock::now();
     {
         std::lock_guard<std::mutex> lock(s->mu);
@@ -294,7 +350,11 @@ extern "C" void iso_server_destroy(iso_server *s)
     s->cv_queue.notify_all();
     for (auto &w : s->workers)
         if (w.thread.joinable()) w.thread.join();
-    for (auto &w : s->workers) iso_ctx_destroy(w.ctx);
+    for (auto &w : s->workers) {
+        if (w.ctx) w.ctx->stream = w.normal;
+        iso_ctx_destroy(w.ctx);
+        if (w.urgent) cudaStreamDestroy(w.urgent);
+    }
     for (auto &kv : s->jobs) delete kv.second;
     delete s;
 }

@@ -29,6 +29,8 @@ DF_LBVH = 1
 DF_TC = 2
 MI_FP64 = 0
 MI_REF32 = 1
+SERVE_FIFO = 0
+SERVE_SHORTEST_FIRST = 1
 MC_REF_DROPPED = 1
 
 
@@ -117,6 +119,7 @@ def _load():
         "iso_server_wait": (C.c_int, [P, C.c_int64, C.POINTER(RequestResult)]),
         "iso_server_get_stats": (C.c_int, [P, C.POINTER(ServerStats)]),
         "iso_server_destroy": (None, [P]),
+        "iso_server_set_policy": (C.c_int, [P, C.c_int, C.c_double]),
         "iso_similarity_map_noalloc": (C.c_int, [P, C.c_int, C.c_int64, C.c_int64, C.c_int, P, P]),
         "iso_pair_map": (C.c_int, [P, P, C.c_int, C.c_int64, C.c_int64, C.c_int, P, C.c_int64, P]),
         "iso_probe_counter_rate": (C.c_int, [P, C.c_int, C.POINTER(C.c_double)]),
@@ -394,6 +397,11 @@ class Server:
         _check(rc)
         mm = res.m
         return ism[: mm * mm].reshape(mm, mm), ids[:mm], res
+
+    def set_policy(self, policy, max_wait_ms=0.0):
+        """SERVE_FIFO or SERVE_SHORTEST_FIRST (smallest work estimate first,
+        the oldest request first once it waited max_wait_ms)."""
+        _check(lib.iso_server_set_policy(self.handle, int(policy), float(max_wait_ms)))
 
     def stats(self):
         st = ServerStats()

@@ -91,3 +91,34 @@ def test_waiters_do_not_hold_memory_the_earliest_needs():
                 ism, _, _ = srv.wait(t)
                 assert np.array_equal(ism, want)
         assert srv.stats().peak_device_bytes <= 100 << 20
+
+
+def test_shortest_first_policy():
+    """Shortest-first serving: the same results as alone (also on the
+    high-priority stream), and small requests queued behind a big one are
+    served before it unless the big one has waited longer than the bound."""
+    import isosim
+    import isosim.synth as synth
+    reqs = requests()
+    with isosim.Context(0) as ctx:
+        alone = [ctx.ism(v, d, i, surface=s, bins=b)[:2] for v, d, i, s, b in reqs]
+    big_vol = synth.gaussian_blobs((96, 96, 96), 6, 7, sigma=(6.0, 18.0))
+    big_iso = synth.inside_isovalues(big_vol, 96)
+    with isosim.Server(0, slots=1, budget_bytes=8 << 30) as srv:
+        srv.set_policy(isosim.SERVE_SHORTEST_FIRST, 60000.0)
+        first = srv.submit(big_vol.ravel(), (96, 96, 96), big_iso, bins=256)  # occupies the one worker
+        queued_big = srv.submit(big_vol.ravel(), (96, 96, 96), big_iso, bins=256)
+        small = [srv.submit(v, d, i, surface=s, bins=b) for v, d, i, s, b in reqs]
+        res_small = [srv.wait(t) for t in small]
+        _, _, r_big = srv.wait(queued_big)
+        srv.wait(first)
+    for k, (ism, ids, res) in enumerate(res_small):
+        assert np.array_equal(ids, alone[k][1]) and np.array_equal(ism, alone[k][0])
+        start = res.queue_ms
+        assert start < r_big.queue_ms, k  # every small one started before the queued big one
+    with isosim.Server(0, slots=3, budget_bytes=2 << 30) as srv:
+        srv.set_policy(isosim.SERVE_SHORTEST_FIRST, 0.0)  # bound 0: the oldest always goes first
+        tickets = [srv.submit(v, d, i, surface=s, bins=b) for v, d, i, s, b in reqs * 2]
+        for k, t in enumerate(tickets):
+            ism, ids, _ = srv.wait(t)
+            assert np.array_equal(ism, alone[k % len(reqs)][0])
