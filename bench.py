@@ -726,7 +726,15 @@ def run_case(case, hist_seg=None):
     ctx = isosim.Context(0)
     if hist_seg is not None:
         ctx.set_hist_segment_values(hist_seg)
-    if case == "ism-128":
+    if case == "tc-small":
+        # one surface of the 128^3 k^-3 field through the tensor-core distance
+        # kernel (and the LBVH for comparison)
+        vol, isos, _ = synth.config2()
+        pts, _ = ctx.surface_points(vol.ravel(), (128, 128, 128), isos[[50]])
+        pn = (pts[0] / np.float32(128)).astype(np.float32)
+        for _ in range(2):
+            ctx.distance_field(pn, (128, 128, 128), method=isosim.DF_TC)
+    elif case == "ism-128":
         vol, isos, bins = synth.config3(size=128, n=64)
         for _ in range(2):
             ctx.ism(vol.ravel(), (128, 128, 128), isos, bins=bins)
@@ -766,7 +774,7 @@ def main():
     ap.add_argument("--plain-surfaces", type=int, default=2)
     ap.add_argument("--serving-requests", type=int, default=24,
                     help="requests of the serving leg in the default line (0: none)")
-    ap.add_argument("--case", default=None, choices=["hist-small", "pipe-small", "ism-128"],
+    ap.add_argument("--case", default=None, choices=["hist-small", "pipe-small", "ism-128", "tc-small"],
                     help="run a small fixed case twice and exit (profiling target)")
     ap.add_argument("--mode", default="single", choices=["single", "serving", "multi"])
     ap.add_argument("--requests", type=int, default=40)
