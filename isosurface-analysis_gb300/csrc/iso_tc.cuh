@@ -106,6 +106,26 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint3
     return false;
 }
 
+// Plain arrival on an mbarrier (count 1 per call).
+__device__ __forceinline__ void mbar_arrive(uint64_t *mbar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(mbar)) : "memory");
+}
+
+// Minimum of three floats in one instruction (sm_100 family).
+__device__ __forceinline__ float fmin3(float a, float b, float c)
+{
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Named barrier over `count` threads (a multiple of 32).
+__device__ __forceinline__ void named_bar(int id, int count)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
 // 32 consecutive FP32 columns of this thread's TMEM lane (32x32b shape: warp w
 // of a warpgroup reads lanes 32w..32w+31; taddr = base + (32w << 16) + col).
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v)
