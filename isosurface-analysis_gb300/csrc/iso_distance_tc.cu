@@ -130,7 +130,7 @@ struct TcArgs {
     int *error;
 };
 
-__global__ void __launch_bounds__(TC_THREADS) df_tc_kernel(TcArgs a)
+__global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
     unsigned char *sA = sm + SM_A;
@@ -231,26 +231,30 @@ __global__ void __launch_bounds__(TC_THREADS) df_tc_kernel(TcArgs a)
             if (!ok) break;
             tc_fence_after();
             const float4 *sP = reinterpret_cast<const float4 *>(sm + SM_P0) + st * TC_POINTS;
-#pragma unroll 1
-            for (int ch = 0; ch < TC_POINTS / 32; ++ch) {
-                float v[32];
-                tmem_ld32(lane_addr + st * TC_POINTS + 32 * ch, v);
-                float m[11];
+            // all 128 accumulators of the block in one round trip
+            uint32_t r[TC_POINTS];
 #pragma unroll
-                for (int k = 0; k < 10; ++k) m[k] = fmin3(v[3 * k], v[3 * k + 1], v[3 * k + 2]);
-                m[10] = fminf(v[30], v[31]);
-                const float cm = fminf(fmin3(fmin3(m[0], m[1], m[2]), fmin3(m[3], m[4], m[5]),
-                                             fmin3(m[6], m[7], m[8])),
-                                       fminf(m[9], m[10]));
-                if (cm <= thr) {
-                    bapprox = fminf(bapprox, cm);
-                    thr = bapprox + tau_of(bapprox, s2, sn);
+            for (int ch = 0; ch < TC_POINTS / 32; ++ch) tmem_ld32_async(lane_addr + st * TC_POINTS + 32 * ch, r + 32 * ch);
+            tmem_wait_ld128(r);
+            float m[43];
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        if (v[j] <= thr) {
-                            const float4 p = sP[32 * ch + j];
-                            best = fminf(best, iso_dist2(__fsub_rn(s.x, p.x), __fsub_rn(s.y, p.y), __fsub_rn(s.z, p.z)));
-                        }
+            for (int k = 0; k < 42; ++k)
+                m[k] = fmin3(__uint_as_float(r[3 * k]), __uint_as_float(r[3 * k + 1]), __uint_as_float(r[3 * k + 2]));
+            m[42] = fminf(__uint_as_float(r[126]), __uint_as_float(r[127]));
+#pragma unroll
+            for (int k = 0; k < 14; ++k) m[k] = fmin3(m[3 * k], m[3 * k + 1], m[3 * k + 2]);
+            m[14] = m[42];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) m[k] = fmin3(m[3 * k], m[3 * k + 1], m[3 * k + 2]);
+            const float cm = fminf(fmin3(m[0], m[1], m[2]), fminf(m[3], m[4]));
+            if (cm <= thr) {
+                bapprox = fminf(bapprox, cm);
+                thr = bapprox + tau_of(bapprox, s2, sn);
+#pragma unroll
+                for (int j = 0; j < TC_POINTS; ++j) {
+                    if (__uint_as_float(r[j]) <= thr) {
+                        const float4 p = sP[j];
+                        best = fminf(best, iso_dist2(__fsub_rn(s.x, p.x), __fsub_rn(s.y, p.y), __fsub_rn(s.z, p.z)));
                     }
                 }
             }
