@@ -679,12 +679,15 @@ struct SegArgs {
     int group;           // pairs whose segments run together (their histograms stay in L2)
     uint32_t *ghist;     // num_pairs x bins*bins
     unsigned int *counter;
+    // precomputed row buckets (row_code_kernel) of the fields of fa and fb,
+    // or null: then every pair computes both buckets from the values
+    const uint32_t *codes_a, *codes_b;
 };
 
-// Wrap corrections straight into the pair's global histogram (see count4).
-__device__ __noinline__ void log_wrap_global(uint32_t *gh, int bin, uint32_t odd, uint32_t old)
+// Wrap corrections straight into the pair's global histogram (see count4):
+// lo and hi are the global indices of the word's low and high counters.
+__device__ __noinline__ void log_wrap_global(uint32_t *gh, int lo, int hi, uint32_t odd, uint32_t old)
 {
-    const int lo = bin & ~1, hi = bin | 1;
     if (!odd) {
         atomicAdd(&gh[lo], 65536u);
         atomicAdd(&gh[hi], 0xFFFFFFFFu);  // -1: the carry the high half received
@@ -695,16 +698,144 @@ __device__ __noinline__ void log_wrap_global(uint32_t *gh, int bin, uint32_t odd
 }
 
 // Wraps corrected straight in the pair's global histogram (segment-major
-// kernel).  The global histogram is unpadded: shared counter index
-// row * packed_stride(bins) + col is global index row * bins + col (same parity).
+// kernel).  The global histogram is unpadded, row = bucket of the pair's
+// first field: shared counter (r, c) at index r * packed_stride(bins) + c is
+// global (r, c), or global (c, r) when the shared histogram is transposed
+// (its rows are the pair's second field).
 struct GlobalWrap {
     uint32_t *gh;
     int rs;  // packed_stride(bins)
+    int bins;
+    int transposed;
     __device__ __forceinline__ void operator()(int bin, uint32_t odd, uint32_t old) const
     {
-        log_wrap_global(gh, bin - 2 * PACKED_PAD * (bin / rs), odd, old);
+        const int r = bin / rs, c0 = (bin - r * rs) & ~1;
+        if (transposed) log_wrap_global(gh, c0 * bins + r, (c0 + 1) * bins + r, odd, old);
+        else log_wrap_global(gh, r * bins + c0, r * bins + c0 + 1, odd, old);
     }
 };
+
+// ---- precomputed row buckets ----------------------------------------------
+// For the segment-major schedule a field's bucket is computed once and reused
+// by every pair in which that field has the larger maximum M.  Such a pair's
+// interval is [mn, M] with mn between the smallest minimum of all fields
+// (m_lo) and the field's own minimum (m_f), and its bucket of value v is
+// clamp(trunc(RN(RN(v - mn) / RN(RN(M - mn) / bins)))).  RN is monotone, so
+// RN(v - mn) lies in [RN(v - m_f), RN(v - m_lo)], the step in
+// [RN(RN(M - m_f)/bins), RN(RN(M - m_lo)/bins)], and the quotient, monotone in
+// both, in [RN(d_lo / s_hi), RN(d_hi / s_lo)]: where both ends give the same
+// bucket, that is the bucket for every such pair.  The code is that bucket
+// times the shared-histogram row stride, or CODE_UNSTABLE (the pair then
+// divides, as for any other value near a bucket edge).
+constexpr uint32_t CODE_UNSTABLE = 0x80000000u;
+
+__global__ void min_of_mins_kernel(const uint32_t *mma, int ma, const uint32_t *mmb, int mb, uint32_t *out)
+{
+    // minima are non-negative floats: their bit patterns order like the values
+    uint32_t v = 0xffffffffu;
+    for (int k = threadIdx.x; k < ma; k += blockDim.x) v = min(v, mma[2 * k]);
+    for (int k = threadIdx.x; k < mb; k += blockDim.x) v = min(v, mmb[2 * k]);
+    v = __reduce_min_sync(0xffffffffu, v);
+    __shared__ uint32_t red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        uint32_t u = threadIdx.x < (blockDim.x + 31) / 32 ? red[threadIdx.x] : 0xffffffffu;
+        u = __reduce_min_sync(0xffffffffu, u);
+        if (threadIdx.x == 0) *out = u;
+    }
+}
+
+__global__ void row_code_kernel(const float *fields, int64_t n, int64_t stride, const uint32_t *minmax,
+                                const uint32_t *m_lo_bits, int bins, int rs, uint32_t *codes)
+{
+    const int f = blockIdx.y;
+    const float mf = bits_to_float(minmax[2 * f]), M = bits_to_float(minmax[2 * f + 1]);
+    const float mlo = bits_to_float(*m_lo_bits);
+    const float s_lo = __fdiv_rn(__fsub_rn(M, mf), (float)bins), s_hi = __fdiv_rn(__fsub_rn(M, mlo), (float)bins);
+    const bool usable = s_lo >= 1.17549435e-38f && isfinite(s_hi) && mlo <= mf;
+    const float *src = fields + (size_t)f * stride;
+    uint32_t *dst = codes + (size_t)f * stride;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const float x = src[v];
+        uint32_t code = CODE_UNSTABLE;
+        if (usable && x == x) {
+            const float q_lo = __fdiv_rn(__fsub_rn(x, mf), s_hi), q_hi = __fdiv_rn(__fsub_rn(x, mlo), s_lo);
+            int b_lo = __float2int_rz(q_lo), b_hi = __float2int_rz(q_hi);
+            b_lo = b_lo >= bins ? bins - 1 : (b_lo < 0 ? 0 : b_lo);
+            b_hi = b_hi >= bins ? bins - 1 : (b_hi < 0 ? 0 : b_hi);
+            if (b_lo == b_hi && q_lo >= 0.0f) code = (uint32_t)(b_lo * rs);
+        }
+        dst[v] = code;
+    }
+}
+
+// As stream_values, with the first side's buckets read from its codes: the
+// second side's buckets come from the bracketed floors, and any voxel whose
+// code is CODE_UNSTABLE or whose floors disagree takes the divisions of both
+// sides (from the values, reloaded from fcode and fother).
+template <int FB, int FRS, bool CSTEP, class Count>
+__device__ __forceinline__ void stream_coded(const Binner &bn, const uint32_t *codes, const float *fcode,
+                                             const float *fother, int64_t v0, int64_t v1, const Count &count)
+{
+    const uint4 *pc = reinterpret_cast<const uint4 *>(codes + v0);
+    const float4 *p1 = reinterpret_cast<const float4 *>(fcode + v0);
+    const float4 *p2 = reinterpret_cast<const float4 *>(fother + v0);
+    const int bins = FB ? FB : bn.bins;
+    const int rstride = FRS ? FRS : bn.rstride;
+    const int n4 = (int)((v1 - v0) >> 2);
+    const int step = CSTEP ? HIST_THREADS : (int)blockDim.x;
+    const float2 nm = make_float2(-bn.mn, -bn.mn);
+    const float2 rl = make_float2(bn.rlo, bn.rlo), nrh = make_float2(-bn.rhi, -bn.rhi);
+    const float2 pb = make_float2(FLOOR_BASE, FLOOR_BASE), nb = make_float2(-FLOOR_BASE, -FLOOR_BASE);
+    const uint32_t top = (uint32_t)(bins - 1);
+    int q = (int)threadIdx.x;
+    uint4 ca = make_uint4(0u, 0u, 0u, 0u), cb = ca;
+    float4 ya = make_float4(0.f, 0.f, 0.f, 0.f), yb = ya;
+    if (q < n4) {
+        ca = __ldg(pc + q);
+        ya = __ldg(p2 + q);
+    }
+    auto bin_and_count = [&](const uint4 &c, const float4 &y, int qq) {
+        const float2 dy01 = __fadd2_rn(make_float2(y.x, y.y), nm), dy23 = __fadd2_rn(make_float2(y.z, y.w), nm);
+        const float2 ly01 = __ffma2_rd(dy01, rl, pb), ly23 = __ffma2_rd(dy23, rl, pb);
+        const float2 hy01 = __ffma2_ru(dy01, nrh, nb), hy23 = __ffma2_ru(dy23, nrh, nb);
+        const float2 zy01 = __fadd2_rn(ly01, hy01), zy23 = __fadd2_rn(ly23, hy23);
+        int b0 = (int)(c.x + min(__float_as_uint(ly01.x) - FLOOR_BASE_BITS, top));
+        int b1 = (int)(c.y + min(__float_as_uint(ly01.y) - FLOOR_BASE_BITS, top));
+        int b2 = (int)(c.z + min(__float_as_uint(ly23.x) - FLOOR_BASE_BITS, top));
+        int b3 = (int)(c.w + min(__float_as_uint(ly23.y) - FLOOR_BASE_BITS, top));
+        const bool slow = (((c.x | c.y | c.z | c.w) & CODE_UNSTABLE) |
+                           (__float_as_uint(zy01.x) | __float_as_uint(zy01.y) | __float_as_uint(zy23.x) |
+                            __float_as_uint(zy23.y))) != 0u;
+        if (__builtin_expect(slow, 0)) {
+            const int4 e = exact_bins4_at(bn.mn, bn.step, bins, rstride, p1, p2, qq);
+            b0 = e.x;
+            b1 = e.y;
+            b2 = e.z;
+            b3 = e.w;
+        }
+        count.add4(b0, b1, b2, b3);
+    };
+    while (q < n4) {
+        const int qb = q + step;
+        if (qb < n4) {
+            cb = __ldg(pc + qb);
+            yb = __ldg(p2 + qb);
+        }
+        bin_and_count(ca, ya, q);
+        if (qb >= n4) break;
+        const int qa = qb + step;
+        if (qa < n4) {
+            ca = __ldg(pc + qa);
+            ya = __ldg(p2 + qa);
+        }
+        bin_and_count(cb, yb, qb);
+        q = qa;
+    }
+    for (int64_t v = v0 + ((int64_t)n4 << 2) + threadIdx.x; v < v1; v += step)
+        count.add1(exact_bucket(bn, fcode[v]) * bn.rstride + exact_bucket(bn, fother[v]));
+}
 
 template <int FB, bool CSTEP, bool RELOAD>
 __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_seg_kernel(SegArgs a)
@@ -747,17 +878,32 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_seg_kernel(Se
         // the segment as a range of its own (same loop code as one pair per CTA)
         const float *f1 = a.fa + (size_t)i * a.stride + v0;
         const float *f2 = a.fb + (size_t)j * a.stride + v0;
-        const Counter<GlobalWrap> cnt{words, GlobalWrap{gh, rs}};
-        if (bn.mode == 0) stream_values<0, FB, FRS, CSTEP, RELOAD>(bn, f1, f2, 0, v1 - v0, cnt);
-        else stream_values<1, FB, FRS, CSTEP, RELOAD>(bn, f1, f2, 0, v1 - v0, cnt);
+        // with codes, the field with the larger maximum reads its codes and
+        // indexes the shared rows; the histogram is transposed when that is the
+        // pair's second field
+        const bool coded = a.codes_a != nullptr && bn.mode == 0;
+        const bool transposed = coded && bits_to_float(a.mmb[2 * j + 1]) > bits_to_float(a.mma[2 * i + 1]);
+        const Counter<GlobalWrap> cnt{words, GlobalWrap{gh, rs, bins, transposed ? 1 : 0}};
+        if (coded) {
+            if (transposed)
+                stream_coded<FB, FRS, CSTEP>(bn, a.codes_b + (size_t)j * a.stride + v0, f2, f1, 0, v1 - v0, cnt);
+            else
+                stream_coded<FB, FRS, CSTEP>(bn, a.codes_a + (size_t)i * a.stride + v0, f1, f2, 0, v1 - v0, cnt);
+        } else if (bn.mode == 0) {
+            stream_values<0, FB, FRS, CSTEP, RELOAD>(bn, f1, f2, 0, v1 - v0, cnt);
+        } else {
+            stream_values<1, FB, FRS, CSTEP, RELOAD>(bn, f1, f2, 0, v1 - v0, cnt);
+        }
         __syncthreads();
         for (int w = threadIdx.x; w < nwords; w += blockDim.x) {
             const uint32_t val = words[w];
             if (val) {  // the pad words stay 0
                 words[w] = 0;
-                const int g = 2 * (w - PACKED_PAD * (w / wps));  // global index of the word's low counter
-                if (val & 0xffffu) atomicAdd(&gh[g], val & 0xffffu);
-                if (val >> 16) atomicAdd(&gh[g + 1], val >> 16);
+                const int r = w / wps, c = 2 * (w - r * wps);  // the word's low counter (r, c)
+                const int glo = transposed ? c * bins + r : r * bins + c;
+                const int ghi = transposed ? glo + bins : glo + 1;
+                if (val & 0xffffu) atomicAdd(&gh[glo], val & 0xffffu);
+                if (val >> 16) atomicAdd(&gh[ghi], val >> 16);
             }
         }
         __syncthreads();
@@ -1095,6 +1241,31 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
         const int group = (int)std::max<size_t>(1, std::min<size_t>(1024, ((size_t)32 << 20) / hist_bytes));
         void *d_gh;
         ISO_TRY(iso_buf(ctx, BUF_HIST_DUMP_SEG, (size_t)chunk * hist_bytes, &d_gh));
+        // precomputed row buckets of both field sets (one set when the pairs
+        // are taken within one), with the smallest minimum of all fields
+        const bool one_set = fb == d_fields_a && mmb == d_minmax_a;
+        const int nsets = one_set ? 1 : 2;
+        void *d_codes, *d_mlo;
+        ISO_TRY(iso_buf(ctx, BUF_ROW_CODES, (size_t)nsets * m * stride * sizeof(uint32_t), &d_codes));
+        ISO_TRY(iso_buf(ctx, BUF_MISC, 256, &d_mlo));
+        min_of_mins_kernel<<<1, 256, 0, ctx->stream>>>(d_minmax_a, m, one_set ? nullptr : mmb, one_set ? 0 : m,
+                                                       (uint32_t *)d_mlo);
+        ISO_LAUNCHED(ctx);
+        uint32_t *codes_a = (uint32_t *)d_codes;
+        uint32_t *codes_b = one_set ? codes_a : codes_a + (size_t)m * stride;
+        {
+            const int64_t per = (n + 255) / 256;
+            const unsigned gx = (unsigned)(per < 512 ? (per < 1 ? 1 : per) : 512);
+            row_code_kernel<<<dim3(gx, m), 256, 0, ctx->stream>>>(d_fields_a, n, stride, d_minmax_a,
+                                                                  (const uint32_t *)d_mlo, bins, packed_stride(bins),
+                                                                  codes_a);
+            ISO_LAUNCHED(ctx);
+            if (!one_set) {
+                row_code_kernel<<<dim3(gx, m), 256, 0, ctx->stream>>>(fb, n, stride, mmb, (const uint32_t *)d_mlo,
+                                                                      bins, packed_stride(bins), codes_b);
+                ISO_LAUNCHED(ctx);
+            }
+        }
         int per_sm_seg = 0;
         ISO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_seg, seg_kernel, HIST_THREADS, smem));
         if (per_sm_seg < 1) per_sm_seg = 1;
@@ -1117,6 +1288,8 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
             sa.group = std::min(group, np);
             sa.ghist = (uint32_t *)d_gh;
             sa.counter = (unsigned int *)d_counter;
+            sa.codes_a = codes_a;
+            sa.codes_b = codes_b;
             const int64_t seg_tasks = (int64_t)np * num_segs;
             const int grid_seg = (int)std::min<int64_t>((int64_t)ctx->num_sms * per_sm_seg, seg_tasks);
             seg_kernel<<<grid_seg, HIST_THREADS, smem, ctx->stream>>>(sa);

@@ -89,6 +89,7 @@ enum IsoBuf {
     BUF_CLNC,            // c*ln(c) for c < 65536, FP64
     BUF_HIST_DUMP_SEG,   // per-pair global histograms of the segment-major schedule
     BUF_SURF_BLOCK_COUNTS,  // marching cubes: per block and isovalue, the vertex versions it counted
+    BUF_ROW_CODES,          // segment-major histograms: per field and value, its precomputed row bucket
     BUF_COUNT_
 };
 
