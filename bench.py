@@ -165,6 +165,8 @@ def run_ours(args):
     ctx = isosim.Context(local)
     if getattr(args, "hist_seg", None) is not None:
         ctx.set_hist_segment_values(args.hist_seg)
+    if args.hist_codes is not None:
+        ctx.set_hist_row_codes(args.hist_codes)
     stream = torch.cuda.ExternalStream(ctx.stream)
     d_vol = torch.from_numpy(vol.ravel()).to(f"cuda:{local}")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
@@ -716,7 +718,7 @@ def run_multi(args):
         pg.destroy_process_group()
 
 
-def run_case(case, hist_seg=None):
+def run_case(case, hist_seg=None, hist_codes=None):
     """Small fixed workloads for kernel profiles: 'hist-small' = similarity
     map of 16 distance-like fields of 128^3 values at 256 bins; 'pipe-small' =
     the 64^3, 32-isovalue, 128-bin pipeline; 'ism-128' = the 128^3 blob+noise
@@ -726,7 +728,15 @@ def run_case(case, hist_seg=None):
     ctx = isosim.Context(0)
     if hist_seg is not None:
         ctx.set_hist_segment_values(hist_seg)
-    if case == "tc-small":
+    if hist_codes is not None:
+        ctx.set_hist_row_codes(hist_codes)
+    if case == "seg-small":
+        # 160^3 blob + noise volume, 32 isovalues, 256 bins: fields of 4,096,000
+        # values, two segments each (the segment-major kernels)
+        vol, isos, bins = synth.config3(size=160, n=32)
+        for _ in range(2):
+            ctx.ism(vol.ravel(), (160, 160, 160), isos, bins=bins)
+    elif case == "tc-small":
         # one surface of the 128^3 k^-3 field through the tensor-core distance
         # kernel (and the LBVH for comparison)
         vol, isos, _ = synth.config2()
@@ -771,10 +781,12 @@ def main():
                     help="sample size of each reference-arm step (see cpu_baseline)")
     ap.add_argument("--no-plain", action="store_true", help="skip the brute-force plain-path leg")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes (no autotuner)")
+    ap.add_argument("--hist-codes", type=int, default=None, choices=[0, 1],
+                    help="segment-major histograms with (1) or without (0) precomputed row buckets")
     ap.add_argument("--plain-surfaces", type=int, default=2)
     ap.add_argument("--serving-requests", type=int, default=24,
                     help="requests of the serving leg in the default line (0: none)")
-    ap.add_argument("--case", default=None, choices=["hist-small", "pipe-small", "ism-128", "tc-small"],
+    ap.add_argument("--case", default=None, choices=["hist-small", "pipe-small", "ism-128", "tc-small", "seg-small"],
                     help="run a small fixed case twice and exit (profiling target)")
     ap.add_argument("--mode", default="single", choices=["single", "serving", "multi"])
     ap.add_argument("--requests", type=int, default=40)
@@ -786,7 +798,7 @@ def main():
     ap.add_argument("--size", type=int, default=128)
     args = ap.parse_args()
     if args.case:
-        run_case(args.case, args.hist_seg)
+        run_case(args.case, args.hist_seg, args.hist_codes)
     elif args.mode == "serving":
         run_serving(args)
     elif args.mode == "multi":

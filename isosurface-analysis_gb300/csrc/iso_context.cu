@@ -114,6 +114,10 @@ extern "C" int iso_ctx_set_limit(iso_ctx *ctx, int which, int64_t value)
             return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: query run must be 0, 8, 16, 32 or 64");
         ctx->query_run = (int)value;
         return ISO_OK;
+    case ISO_LIMIT_HIST_ROW_CODES:
+        if (value != 0 && value != 1) return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: row codes must be 0 or 1");
+        ctx->hist_row_codes = (int)value;
+        return ISO_OK;
     case ISO_LIMIT_MI_MODE:
         if (value != ISO_MI_FP64 && value != ISO_MI_REF32)
             return iso_fail(ISO_ERR_ARG, "iso_ctx_set_limit: unknown MI mode %lld", (long long)value);

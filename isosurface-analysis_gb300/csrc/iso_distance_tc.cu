@@ -6,34 +6,40 @@
 // of isosurfaces_cuda/src/DistanceField.cu:49-65 and the nearest query of
 // isosurfaces_cuda/src/BVH.cu:577-613).
 //
-// One CTA owns a brick of 128 samples (8 z x 4 y x 4 x) of one field and
-// streams the surface's points in blocks of 128:
-//  * both sides are centred on the brick: sigma = s - c per sample, pi = p - c
-//    per point (FP32), so the terms of the contraction shrink with the
-//    distance instead of being O(1), and split into f16 hi + lo parts;
-//  * A (128 x 16, one row per sample):  [sh, sh, sl, 1 1 1, 0...]
-//    B (128 x 16, one row per point):   [-2 ph, -2 pl, -2 ph, q_hi q_mid q_lo, 0...]
-//    so that A.B = |pi|^2 - 2 sigma.pi (the sl*pl products are dropped);
-//    one tcgen05.mma (M = 128, N = 128, K = 16, f16 in, FP32 out) per block
-//    writes a 128 x 128 FP32 tile to tensor memory;
-//  * each thread reads its sample's 128 values back (tcgen05.ld) and keeps the
-//    smallest, B; every point whose value is within tau of B is a candidate,
-//    and its canonical FP32 distance (the fma chain every method uses) is
-//    computed from the original coordinates; the field value is the minimum
-//    over candidates.
+// Operands, built once per surface (tc_prepare_kernel) and per CTA:
+//  * B (one row of 16 f16 per point, in blocks of 128 rows laid out as the
+//    MMA reads them, padding rows of each surface's last block marked):
+//      [-2 ph (3), -2 pl (3), -2 ph (3), q_hi, q_mid, q_lo, 0 x 4]
+//    with p = ph + pl split into f16 parts and q = |p|^2 (FP32) in three;
+//  * A (one row per sample s of the CTA's 8 x 4 x 4 brick):
+//      [sh (3), sh (3), sl (3), 1, 1, 1, 0 x 4]
+//    so that A.B = |p|^2 - 2 s.p = |s - p|^2 - |s|^2 (the sl*pl products are
+//    dropped).  One tcgen05.mma (M 128, N 128, K 16, f16 in, FP32 out) per
+//    block of points writes a 128 x 128 tile to tensor memory.
+//  * One warp streams the blocks: a bulk copy (TMA) brings a block's B rows and
+//    FP32 points into one of two shared-memory stages, and one thread issues
+//    the block's MMA into one of two accumulators once the copy has landed.
+//    Eight warps read the accumulators back (tcgen05.ld): warp w takes the 32
+//    samples of TMEM lane quarter w % 4 and columns 64 (w / 4) .. +63, keeps
+//    the smallest value B of its columns and recomputes the canonical FP32
+//    distance of every point within tau of B; the two halves' minima are
+//    merged at the end.
 //
 // Exactness: the canonical winner w (smallest canonical FP32 distance) is
-// always a candidate, because a(w) - B_final <= |e(w)| + |e(j)| + 1e-6 * D,
-// where a = A.B, e is a's error against the exact |sigma - pi|^2 - |sigma|^2
-// and j the point giving B.  tau bounds that: with D ~ B + |sigma|^2 (the
-// squared distance) and R = |sigma| + sqrt(D) (the radius within which both
-// points lie, measured from the brick centre), the error of a is at most
-// kappa * R^2 (f16 split residuals, the dropped sl*pl terms and FP32
-// accumulation of at most 12 terms of magnitude <= R^2; kappa = 2^-14 is about
-// ten times the bound) plus the rounding of the centring (<= 1e-6 * sqrt(D))
-// and of the f16 parts of |pi|^2 (< 1e-7).  Any other point within tau is
-// also rechecked, so a loose tau costs time, never exactness.
+// always a candidate: with e the error of A.B against the exact
+// |s - p|^2 - |s|^2 and j the point giving B, A.B(w) - B <= |e(w)| + |e(j)|
+// + the rounding of the canonical distances (<= 6e-7 of the squared
+// distance).  |e| <= 12 * 2^-23 * (|s| + |p|)^2 (FP32 accumulation of 12 exact
+// f16 products, allowing truncation) + 2^-20 (|s| + |p|)^2 (f16 split
+// residuals and the dropped terms) + 5e-7 (f16 parts in the subnormal range);
+// tau is twice the sum of two such bounds and the canonical rounding, for the
+// largest |s| of the brick and |p| of the surface.  For coordinates in [0, 1]
+// tau ~ 1.3e-4 in squared normalised units; any other point within tau is
+// also rechecked, so a loose tau costs rechecks (a few dozen per sample),
+// never exactness.
 #include <cuda_fp16.h>
+
+#include <vector>
 
 #include "iso_internal.cuh"
 #include "iso_tc.cuh"
@@ -42,30 +48,25 @@ using namespace isotc;
 
 namespace {
 
-// Warp roles: warps 0-3 own one sample each per thread (A rows, read-back and
-// candidates); warps 4-5 convert the next block of points into the B operand
-// while the tensor cores and the first four warps work on the current one.
-// Two operand stages and two accumulators (2 x 128 TMEM columns) alternate;
-// full[s] completes when the MMA of stage s is done (tcgen05.commit), empty[s]
-// when the four sample warps have read its accumulator and points.
-constexpr int EPI_WARPS = 4;
-constexpr int PROD_WARPS = 2;
-constexpr int TC_THREADS = 32 * (EPI_WARPS + PROD_WARPS);
-constexpr int TC_POINTS = 128;        // points per MMA (N)
-constexpr uint32_t TC_COLS = 256;     // two accumulators of TC_POINTS columns
+constexpr int READ_WARPS = 8;                 // two per TMEM lane quarter
+constexpr int TC_THREADS = 32 * (READ_WARPS + 1);
+constexpr int TC_POINTS = 128;                // points per MMA (N), rows per B block
+constexpr uint32_t TC_COLS = 256;             // two accumulators of TC_POINTS columns
+constexpr int HALF = TC_POINTS / 2;           // columns read back per thread and block
+constexpr int BLOCK_BYTES = TC_POINTS * 32;   // one B block (4 KB)
 constexpr int BRICK_Z = 8, BRICK_Y = 4, BRICK_X = 4;
-// shared memory: A tile, two B stages, two point stages, barriers and the
-// TMEM slot; the dynamic size is padded so that at most two CTAs share an SM
+// shared memory: A tile, two B stages, two point stages, the halves' minima,
+// barriers and the TMEM slot; padded so that at most two CTAs share an SM
 // (2 x 256 TMEM columns = all 512)
 constexpr int SM_A = 0;
-constexpr int SM_B0 = 4096;                          // 128 rows x 32 B per stage
-constexpr int SM_P0 = SM_B0 + 2 * TC_POINTS * 32;    // 128 float4 per stage
-constexpr int SM_BAR = SM_P0 + 2 * TC_POINTS * 16;   // full[2], empty[2], slot
+constexpr int SM_B0 = 4096;
+constexpr int SM_P0 = SM_B0 + 2 * BLOCK_BYTES;        // 128 float4 per stage
+constexpr int SM_BEST = SM_P0 + 2 * TC_POINTS * 16;   // 128 floats
+constexpr int SM_BAR = SM_BEST + 128 * 4;             // loaded[2], full[2], empty[2], slot
 constexpr int SM_USED = SM_BAR + 64;
 constexpr int SM_ALLOC = 80 * 1024;
-constexpr float KAPPA = 6.103515625e-05f;      // 2^-14
-constexpr float SENTINEL_Q = 30000.0f;         // |pi|^2 of padding rows: never within tau
-constexpr uint32_t WAIT_LIMIT = 1u << 26;      // polls of one barrier wait before giving up
+constexpr float SENTINEL_Q = 30000.0f;        // |p|^2 of padding rows: never within tau
+constexpr uint32_t WAIT_LIMIT = 1u << 26;     // polls of one barrier wait before giving up
 
 __device__ __forceinline__ void split_f16(float v, __half &hi, __half &lo)
 {
@@ -81,49 +82,57 @@ __device__ __forceinline__ uint32_t pack_h2(__half lo, __half hi)
 
 __device__ __forceinline__ int64_t clamp_hi(int64_t v, int64_t hi) { return v < hi ? v : hi; }
 
-__device__ __forceinline__ float tau_of(float best, float s2, float sn)
+// B rows of every surface in blocks of TC_POINTS (surface q's first block at
+// block_base[q]); the largest |p| of each surface as float bits in pmax.
+__global__ void tc_prepare_kernel(IsoSegments sg, const int64_t *block_base, int m, unsigned char *bops,
+                                  uint32_t *pmax)
 {
-    const float D = fmaxf(best + s2, 0.0f) + 1e-6f;
-    const float sd = sqrtf(D);
-    const float R = sn + sd;
-    return 1e-6f * D + 2.0f * KAPPA * R * R + 1e-6f * sd + 4e-7f;
-}
-
-// B row of one point (or of padding when `valid` is false) and its FP32 copy.
-__device__ __forceinline__ void write_row(unsigned char *sB, float4 *sP, int r, bool valid, float4 p, float3 c)
-{
-    uint4 w0 = make_uint4(0u, 0u, 0u, 0u), w1 = w0;
-    if (valid) {
-        const float px = __fsub_rn(p.x, c.x), py = __fsub_rn(p.y, c.y), pz = __fsub_rn(p.z, c.z);
-        __half hx, lx, hy, ly, hz, lz;
-        split_f16(px, hx, lx);
-        split_f16(py, hy, ly);
-        split_f16(pz, hz, lz);
-        const __half m2 = __float2half_rn(-2.0f);
-        hx = __hmul(m2, hx);
-        hy = __hmul(m2, hy);
-        hz = __hmul(m2, hz);
-        lx = __hmul(m2, lx);
-        ly = __hmul(m2, ly);
-        lz = __hmul(m2, lz);
-        const float q = __fmaf_rn(pz, pz, __fmaf_rn(py, py, __fmul_rn(px, px)));
-        const __half qh = __float2half_rn(q);
-        const float q1 = __fsub_rn(q, __half2float(qh));
-        const __half qm = __float2half_rn(q1);
-        const __half ql = __float2half_rn(__fsub_rn(q1, __half2float(qm)));
-        w0 = make_uint4(pack_h2(hx, hy), pack_h2(hz, lx), pack_h2(ly, lz), pack_h2(hx, hy));
-        w1 = make_uint4(pack_h2(hz, qh), pack_h2(qm, ql), 0u, 0u);
-    } else {
-        w1.x = pack_h2(__float2half_rn(0.0f), __float2half_rn(SENTINEL_Q));
+    const int q = blockIdx.y;
+    const int64_t P = sg.count[q], padded = (P + TC_POINTS - 1) / TC_POINTS * TC_POINTS;
+    unsigned char *dst = bops + (size_t)block_base[q] * BLOCK_BYTES;
+    float mx = 0.0f;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < padded; r += (int64_t)gridDim.x * blockDim.x) {
+        uint4 w0 = make_uint4(0u, 0u, 0u, 0u), w1 = w0;
+        if (r < P) {
+            const float4 p = sg.points[sg.offset[q] + r];
+            __half hx, lx, hy, ly, hz, lz;
+            split_f16(p.x, hx, lx);
+            split_f16(p.y, hy, ly);
+            split_f16(p.z, hz, lz);
+            const __half m2 = __float2half_rn(-2.0f);
+            hx = __hmul(m2, hx);
+            hy = __hmul(m2, hy);
+            hz = __hmul(m2, hz);
+            lx = __hmul(m2, lx);
+            ly = __hmul(m2, ly);
+            lz = __hmul(m2, lz);
+            const float qq = __fmaf_rn(p.z, p.z, __fmaf_rn(p.y, p.y, __fmul_rn(p.x, p.x)));
+            const __half qh = __float2half_rn(qq);
+            const float q1 = __fsub_rn(qq, __half2float(qh));
+            const __half qm = __float2half_rn(q1);
+            const __half ql = __float2half_rn(__fsub_rn(q1, __half2float(qm)));
+            w0 = make_uint4(pack_h2(hx, hy), pack_h2(hz, lx), pack_h2(ly, lz), pack_h2(hx, hy));
+            w1 = make_uint4(pack_h2(hz, qh), pack_h2(qm, ql), 0u, 0u);
+            mx = fmaxf(mx, qq);
+        } else {
+            w1.x = pack_h2(__float2half_rn(0.0f), __float2half_rn(SENTINEL_Q));
+        }
+        unsigned char *blk = dst + (size_t)(r / TC_POINTS) * BLOCK_BYTES;
+        const uint32_t row = (uint32_t)(r % TC_POINTS);
+        *reinterpret_cast<uint4 *>(blk + tc_offset(row, 0)) = w0;
+        *reinterpret_cast<uint4 *>(blk + tc_offset(row, 8)) = w1;
     }
-    *reinterpret_cast<uint4 *>(sB + tc_offset(r, 0)) = w0;
-    *reinterpret_cast<uint4 *>(sB + tc_offset(r, 8)) = w1;
-    sP[r] = p;
+    // |p|^2 >= 0: float bits order like values
+    mx = sqrtf(mx);
+    atomicMax(&pmax[q], __float_as_uint(mx));
 }
 
 struct TcArgs {
     IsoSampleGrid g;
     IsoSegments sg;
+    const unsigned char *bops;    // prepared B blocks
+    const int64_t *block_base;    // per segment: first B block
+    const uint32_t *pmax;         // per segment: largest |p| (float bits)
     float *fields;
     int64_t stride;
     int bx, by, bz;  // bricks per axis
@@ -134,47 +143,55 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
     unsigned char *sA = sm + SM_A;
-    uint64_t *full = reinterpret_cast<uint64_t *>(sm + SM_BAR);
-    uint64_t *empty = full + 2;
-    uint32_t *slot = reinterpret_cast<uint32_t *>(sm + SM_BAR + 32);
+    float *sBest = reinterpret_cast<float *>(sm + SM_BEST);
+    uint64_t *loaded = reinterpret_cast<uint64_t *>(sm + SM_BAR);
+    uint64_t *full = loaded + 2;
+    uint64_t *empty = loaded + 4;
+    uint32_t *slot = reinterpret_cast<uint32_t *>(sm + SM_BAR + 48);
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
     const int seg = blockIdx.y;
     const int64_t off = a.sg.offset[seg], P = a.sg.count[seg];
     const IsoSampleGrid &g = a.g;
     const int64_t X10 = g.F / (g.Y10 * g.Z10);
 
-    // the brick and its centre
+    // this thread's sample: warp w % 4 covers samples 32 (w % 4) .. + 31
     const int brick = blockIdx.x;
     const int bz = brick % a.bz, by = (brick / a.bz) % a.by, bxi = brick / (a.bz * a.by);
-    const int64_t cx = clamp_hi((int64_t)bxi * BRICK_X + 2, X10 - 1),
-                  cy = clamp_hi((int64_t)by * BRICK_Y + 2, g.Y10 - 1), cz = clamp_hi((int64_t)bz * BRICK_Z + 4, g.Z10 - 1);
-    const float3 c = iso_sample_point(g, (cx * g.Y10 + cy) * g.Z10 + cz);
-
-    // sample warps: this thread's sample and its A row
-    const int ts = t & 127;
+    const int ts = (32 * (w & 3) + lane) & 127;
     const int64_t z = (int64_t)bz * BRICK_Z + (ts & 7), y = (int64_t)by * BRICK_Y + ((ts >> 3) & 3),
                   x = (int64_t)bxi * BRICK_X + (ts >> 5);
-    const bool inside = w < EPI_WARPS && z < g.Z10 && y < g.Y10 && x < X10;
+    const bool inside = z < g.Z10 && y < g.Y10 && x < X10;
     const int64_t idx = inside ? (x * g.Y10 + y) * g.Z10 + z : 0;
     const float3 s = iso_sample_point(g, idx);
-    const float3 sig = make_float3(__fsub_rn(s.x, c.x), __fsub_rn(s.y, c.y), __fsub_rn(s.z, c.z));
-    const float s2 = __fmaf_rn(sig.z, sig.z, __fmaf_rn(sig.y, sig.y, __fmul_rn(sig.x, sig.x)));
-    const float sn = sqrtf(s2);
-    if (w < EPI_WARPS) {
+    if (w < 4) {
         __half hx, lx, hy, ly, hz, lz;
-        split_f16(sig.x, hx, lx);
-        split_f16(sig.y, hy, ly);
-        split_f16(sig.z, hz, lz);
+        split_f16(s.x, hx, lx);
+        split_f16(s.y, hy, ly);
+        split_f16(s.z, hz, lz);
         const __half one = __float2half_rn(1.0f);
         *reinterpret_cast<uint4 *>(sA + tc_offset(ts, 0)) =
             make_uint4(pack_h2(hx, hy), pack_h2(hz, hx), pack_h2(hy, hz), pack_h2(lx, ly));
         *reinterpret_cast<uint4 *>(sA + tc_offset(ts, 8)) = make_uint4(pack_h2(lz, one), pack_h2(one, one), 0u, 0u);
     }
+    // tau from the largest |s| of the brick (its far corner from the origin)
+    // and the surface's largest |p|
+    float tau;
+    {
+        const int64_t xc = clamp_hi((int64_t)bxi * BRICK_X + BRICK_X - 1, X10 - 1),
+                      yc = clamp_hi((int64_t)by * BRICK_Y + BRICK_Y - 1, g.Y10 - 1),
+                      zc = clamp_hi((int64_t)bz * BRICK_Z + BRICK_Z - 1, g.Z10 - 1);
+        const float3 corner = iso_sample_point(g, (xc * g.Y10 + yc) * g.Z10 + zc);
+        const float smax = sqrtf(corner.x * corner.x + corner.y * corner.y + corner.z * corner.z) * 1.0001f;
+        const float R = smax + __uint_as_float(a.pmax[seg]) * 1.0001f;
+        // twice (the error bound of two values plus the canonical rounding)
+        tau = 2.0f * (2.0f * ((12.0f * 1.1920929e-7f + 9.5367432e-7f) * R * R + 5e-7f) + 6e-7f * R * R);
+    }
     if (t == 0) {
-        mbar_init(&full[0], 1);
-        mbar_init(&full[1], 1);
-        mbar_init(&empty[0], EPI_WARPS);
-        mbar_init(&empty[1], EPI_WARPS);
+        for (int k = 0; k < 2; ++k) {
+            mbar_init(&loaded[k], 1);
+            mbar_init(&full[k], 1);
+            mbar_init(&empty[k], READ_WARPS);
+        }
     }
     if (w == 0) {
         tmem_alloc(slot, TC_COLS);
@@ -186,72 +203,68 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
     tc_fence_after();
     const uint32_t tbase = *slot;
     const int64_t nblocks = (P + TC_POINTS - 1) / TC_POINTS;
+    const unsigned char *bsrc = a.bops + (size_t)a.block_base[seg] * BLOCK_BYTES;
     bool ok = true;
 
-    if (w >= EPI_WARPS) {
-        // producers: 64 rows per warp, two per lane; the next block's points
-        // are loaded while the current one is converted
-        const int pw = w - EPI_WARPS;
-        const uint64_t adesc = tc_desc(sA);
-        const uint32_t idesc = tc_idesc_f16_f32(128, TC_POINTS);
-        const int r0 = pw * 64 + lane, r1 = r0 + 32;
-        float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f), p1 = p0;
-        if (r0 < P) p0 = a.sg.points[off + r0];
-        if (r1 < P) p1 = a.sg.points[off + r1];
-        for (int64_t b = 0; b < nblocks; ++b) {
-            const int st = (int)(b & 1);
-            const int64_t base = b * TC_POINTS;
-            float4 n0 = make_float4(0.f, 0.f, 0.f, 0.f), n1 = n0;
-            if (base + TC_POINTS + r0 < P) n0 = a.sg.points[off + base + TC_POINTS + r0];
-            if (base + TC_POINTS + r1 < P) n1 = a.sg.points[off + base + TC_POINTS + r1];
-            // stage st was last used by block b - 2: wait until it was read
-            if (b >= 2) ok = __all_sync(0xffffffffu, mbar_wait(&empty[st], (uint32_t)(((b >> 1) - 1) & 1), WAIT_LIMIT));
-            if (!ok) break;
-            unsigned char *sB = sm + SM_B0 + st * TC_POINTS * 32;
-            float4 *sP = reinterpret_cast<float4 *>(sm + SM_P0) + st * TC_POINTS;
-            write_row(sB, sP, r0, base + r0 < P, p0, c);
-            write_row(sB, sP, r1, base + r1 < P, p1, c);
-            fence_async_smem();
-            named_bar(1, 32 * PROD_WARPS);
-            if (t == 32 * EPI_WARPS) {
+    if (w == READ_WARPS) {
+        // the streaming warp: one thread copies blocks and issues the MMAs
+        if (lane == 0) {
+            const uint64_t adesc = tc_desc(sA);
+            const uint32_t idesc = tc_idesc_f16_f32(128, TC_POINTS);
+            auto fetch = [&](int64_t b) {
+                const int st = (int)(b & 1);
+                const int64_t cnt = P - b * TC_POINTS < TC_POINTS ? P - b * TC_POINTS : TC_POINTS;
+                mbar_expect_tx(&loaded[st], (uint32_t)(BLOCK_BYTES + cnt * 16));
+                bulk_g2s(sm + SM_B0 + st * BLOCK_BYTES, bsrc + (size_t)b * BLOCK_BYTES, BLOCK_BYTES, &loaded[st]);
+                bulk_g2s(sm + SM_P0 + st * TC_POINTS * 16, a.sg.points + off + b * TC_POINTS, (uint32_t)(cnt * 16),
+                         &loaded[st]);
+            };
+            fetch(0);
+            if (nblocks > 1) fetch(1);
+            for (int64_t b = 0; b < nblocks && ok; ++b) {
+                const int st = (int)(b & 1);
+                ok = mbar_wait(&loaded[st], (uint32_t)((b >> 1) & 1), WAIT_LIMIT);
+                if (!ok) break;
                 tc_fence_after();
-                tc_mma_f16(tbase + st * TC_POINTS, adesc, tc_desc(sB), idesc, 0);
+                tc_mma_f16(tbase + st * TC_POINTS, adesc, tc_desc(sm + SM_B0 + st * BLOCK_BYTES), idesc, 0);
                 tc_commit(&full[st]);
+                // refill the other stage with block b + 1 once block b - 1 has
+                // been read back (its accumulator is then free for MMA b + 1)
+                if (b >= 1 && b + 1 < nblocks) {
+                    ok = mbar_wait(&empty[st ^ 1], (uint32_t)(((b - 1) >> 1) & 1), WAIT_LIMIT);
+                    if (ok) fetch(b + 1);
+                }
             }
-            p0 = n0;
-            p1 = n1;
         }
+        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
     } else {
-        float best = ISO_DF_INIT_BOUND;  // exact canonical minimum
+        float best = ISO_DF_INIT_BOUND;  // exact canonical minimum over this thread's columns
         float bapprox = __int_as_float(0x7f800000), thr = bapprox;
-        const uint32_t lane_addr = tbase + ((uint32_t)(32 * w) << 16);
+        const int col0 = HALF * (w >> 2);
+        const uint32_t lane_addr = tbase + ((uint32_t)(32 * (w & 3)) << 16) + col0;
         for (int64_t b = 0; b < nblocks; ++b) {
             const int st = (int)(b & 1);
             ok = __all_sync(0xffffffffu, mbar_wait(&full[st], (uint32_t)((b >> 1) & 1), WAIT_LIMIT));
             if (!ok) break;
             tc_fence_after();
-            const float4 *sP = reinterpret_cast<const float4 *>(sm + SM_P0) + st * TC_POINTS;
-            // all 128 accumulators of the block in one round trip
-            uint32_t r[TC_POINTS];
+            uint32_t r[HALF];
+            tmem_ld32_async(lane_addr + st * TC_POINTS, r);
+            tmem_ld32_async(lane_addr + st * TC_POINTS + 32, r + 32);
+            tmem_wait_ld64(r);
+            float mm[22];
 #pragma unroll
-            for (int ch = 0; ch < TC_POINTS / 32; ++ch) tmem_ld32_async(lane_addr + st * TC_POINTS + 32 * ch, r + 32 * ch);
-            tmem_wait_ld128(r);
-            float m[43];
+            for (int k = 0; k < 21; ++k)
+                mm[k] = fmin3(__uint_as_float(r[3 * k]), __uint_as_float(r[3 * k + 1]), __uint_as_float(r[3 * k + 2]));
+            mm[21] = __uint_as_float(r[63]);
 #pragma unroll
-            for (int k = 0; k < 42; ++k)
-                m[k] = fmin3(__uint_as_float(r[3 * k]), __uint_as_float(r[3 * k + 1]), __uint_as_float(r[3 * k + 2]));
-            m[42] = fminf(__uint_as_float(r[126]), __uint_as_float(r[127]));
-#pragma unroll
-            for (int k = 0; k < 14; ++k) m[k] = fmin3(m[3 * k], m[3 * k + 1], m[3 * k + 2]);
-            m[14] = m[42];
-#pragma unroll
-            for (int k = 0; k < 5; ++k) m[k] = fmin3(m[3 * k], m[3 * k + 1], m[3 * k + 2]);
-            const float cm = fminf(fmin3(m[0], m[1], m[2]), fminf(m[3], m[4]));
+            for (int k = 0; k < 7; ++k) mm[k] = fmin3(mm[3 * k], mm[3 * k + 1], mm[3 * k + 2]);
+            const float cm = fminf(fmin3(fmin3(mm[0], mm[1], mm[2]), fmin3(mm[3], mm[4], mm[5]), mm[6]), mm[21]);
             if (cm <= thr) {
                 bapprox = fminf(bapprox, cm);
-                thr = bapprox + tau_of(bapprox, s2, sn);
+                thr = bapprox + tau;
+                const float4 *sP = reinterpret_cast<const float4 *>(sm + SM_P0) + st * TC_POINTS + col0;
 #pragma unroll
-                for (int j = 0; j < TC_POINTS; ++j) {
+                for (int j = 0; j < HALF; ++j) {
                     if (__uint_as_float(r[j]) <= thr) {
                         const float4 p = sP[j];
                         best = fminf(best, iso_dist2(__fsub_rn(s.x, p.x), __fsub_rn(s.y, p.y), __fsub_rn(s.z, p.z)));
@@ -262,9 +275,12 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[st]);
         }
-        if (ok && inside) a.fields[(size_t)seg * a.stride + idx] = iso_df_finish(best, P);
+        if (w >= 4) sBest[ts] = best;
+        named_bar(1, 32 * READ_WARPS);
+        if (w < 4 && ok && inside)
+            a.fields[(size_t)seg * a.stride + idx] = iso_df_finish(fminf(best, sBest[ts]), P);
     }
-    if (!ok && (t & 31) == 0) atomicExch(a.error, 1);
+    if (!ok && lane == 0) atomicExch(a.error, 1);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -276,37 +292,51 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
 int iso_run_distance_tc(iso_ctx *ctx, const IsoSampleGrid &g, const IsoSegments &sg, const int64_t *h_seg_count, int m,
                         float *fields, int64_t stride)
 {
-    (void)h_seg_count;
     static_assert(SM_USED <= SM_ALLOC, "shared memory layout");
     const int64_t X10 = g.F / (g.Y10 * g.Z10);
+    // prepared B blocks of every surface
+    std::vector<int64_t> base((size_t)m + 1, 0);
+    for (int q = 0; q < m; ++q) base[q + 1] = base[q] + (h_seg_count[q] + TC_POINTS - 1) / TC_POINTS;
+    void *d_bops, *d_base, *d_pmax, *d_err;
+    ISO_TRY(iso_buf(ctx, BUF_TC_OPERANDS, (size_t)base[m] * BLOCK_BYTES, &d_bops));
+    ISO_TRY(iso_buf(ctx, BUF_STAGING_A, (size_t)(m + 1) * sizeof(int64_t) + (size_t)m * sizeof(uint32_t) + 256,
+                    &d_base));
+    d_pmax = (char *)d_base + ((size_t)(m + 1) * sizeof(int64_t) + 255) / 256 * 256;
+    ISO_CUDA(cudaMemcpyAsync(d_base, base.data(), (size_t)(m + 1) * sizeof(int64_t), cudaMemcpyHostToDevice,
+                             ctx->stream));
+    ISO_CUDA(cudaMemsetAsync(d_pmax, 0, (size_t)m * sizeof(uint32_t), ctx->stream));
+    ISO_TRY(iso_buf(ctx, BUF_TASK_COUNTER, 256, &d_err));
+    int *err_flag = (int *)d_err + 2;
+    ISO_CUDA(cudaMemsetAsync(err_flag, 0, sizeof(int), ctx->stream));
+    ISO_CUDA(cudaFuncSetAttribute(df_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_ALLOC));
     TcArgs a;
     a.g = g;
-    a.sg = sg;
-    a.fields = fields;
     a.stride = stride;
     a.bz = (int)((g.Z10 + BRICK_Z - 1) / BRICK_Z);
     a.by = (int)((g.Y10 + BRICK_Y - 1) / BRICK_Y);
     a.bx = (int)((X10 + BRICK_X - 1) / BRICK_X);
+    a.error = err_flag;
     const int64_t bricks = (int64_t)a.bx * a.by * a.bz;
     if (bricks > 0x7fffffff) return iso_fail(ISO_ERR_ARG, "tensor-core distance: grid too large");
-    void *d_err;
-    ISO_TRY(iso_buf(ctx, BUF_TASK_COUNTER, 256, &d_err));
-    a.error = (int *)d_err + 2;
-    ISO_CUDA(cudaMemsetAsync(a.error, 0, sizeof(int), ctx->stream));
-    ISO_CUDA(cudaFuncSetAttribute(df_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_ALLOC));
-    for (int base = 0; base < m; base += 65535) {
-        const int cnt = m - base < 65535 ? m - base : 65535;
+    for (int q0 = 0; q0 < m; q0 += 65535) {
+        const int cnt = m - q0 < 65535 ? m - q0 : 65535;
         IsoSegments s2 = sg;
-        s2.offset = sg.offset + base;
-        s2.count = sg.count + base;
+        s2.offset = sg.offset + q0;
+        s2.count = sg.count + q0;
+        tc_prepare_kernel<<<dim3(64, cnt), 256, 0, ctx->stream>>>(s2, (const int64_t *)d_base + q0, cnt,
+                                                                  (unsigned char *)d_bops, (uint32_t *)d_pmax + q0);
+        ISO_LAUNCHED(ctx);
         a.sg = s2;
-        a.fields = fields + (size_t)base * stride;
+        a.bops = (const unsigned char *)d_bops;
+        a.block_base = (const int64_t *)d_base + q0;
+        a.pmax = (const uint32_t *)d_pmax + q0;
+        a.fields = fields + (size_t)q0 * stride;
         df_tc_kernel<<<dim3((unsigned)bricks, cnt), TC_THREADS, SM_ALLOC, ctx->stream>>>(a);
         ISO_LAUNCHED(ctx);
     }
     int err = 0;
-    ISO_CUDA(cudaMemcpyAsync(&err, a.error, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    ISO_CUDA(cudaMemcpyAsync(&err, err_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     ISO_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (err) return iso_fail(ISO_ERR_INTERNAL, "tensor-core distance: an MMA did not complete");
+    if (err) return iso_fail(ISO_ERR_INTERNAL, "tensor-core distance: a copy or an MMA did not complete");
     return ISO_OK;
 }

@@ -1245,15 +1245,16 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
         // are taken within one), with the smallest minimum of all fields
         const bool one_set = fb == d_fields_a && mmb == d_minmax_a;
         const int nsets = one_set ? 1 : 2;
-        void *d_codes, *d_mlo;
-        ISO_TRY(iso_buf(ctx, BUF_ROW_CODES, (size_t)nsets * m * stride * sizeof(uint32_t), &d_codes));
-        ISO_TRY(iso_buf(ctx, BUF_MISC, 256, &d_mlo));
-        min_of_mins_kernel<<<1, 256, 0, ctx->stream>>>(d_minmax_a, m, one_set ? nullptr : mmb, one_set ? 0 : m,
-                                                       (uint32_t *)d_mlo);
-        ISO_LAUNCHED(ctx);
-        uint32_t *codes_a = (uint32_t *)d_codes;
-        uint32_t *codes_b = one_set ? codes_a : codes_a + (size_t)m * stride;
-        {
+        uint32_t *codes_a = nullptr, *codes_b = nullptr;
+        if (ctx->hist_row_codes) {
+            void *d_codes, *d_mlo;
+            ISO_TRY(iso_buf(ctx, BUF_ROW_CODES, (size_t)nsets * m * stride * sizeof(uint32_t), &d_codes));
+            ISO_TRY(iso_buf(ctx, BUF_MISC, 256, &d_mlo));
+            min_of_mins_kernel<<<1, 256, 0, ctx->stream>>>(d_minmax_a, m, one_set ? nullptr : mmb, one_set ? 0 : m,
+                                                           (uint32_t *)d_mlo);
+            ISO_LAUNCHED(ctx);
+            codes_a = (uint32_t *)d_codes;
+            codes_b = one_set ? codes_a : codes_a + (size_t)m * stride;
             const int64_t per = (n + 255) / 256;
             const unsigned gx = (unsigned)(per < 512 ? (per < 1 ? 1 : per) : 512);
             row_code_kernel<<<dim3(gx, m), 256, 0, ctx->stream>>>(d_fields_a, n, stride, d_minmax_a,

@@ -302,6 +302,10 @@ class Context:
                                 cache_path.encode() if cache_path else None, C.byref(t)))
         return t
 
+    def set_hist_row_codes(self, on):
+        """Segment-major histograms with precomputed row buckets (1) or not (0)."""
+        _check(lib.iso_ctx_set_limit(self.handle, 7, int(on)))
+
     def set_query_run(self, run):
         """LBVH query samples per lane along x (0: by volume size)."""
         _check(lib.iso_ctx_set_limit(self.handle, 6, int(run)))
