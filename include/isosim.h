@@ -128,9 +128,9 @@ ISO_API int64_t iso_ctx_launches(iso_ctx *ctx);
 #define ISO_LIMIT_QUERY_RUN 6 /* LBVH query: samples each lane sweeps along x, 8, 16, 32 or 64
                                   (0 = by volume size, the default: 64 from 128 samples along x,
                                   else 8); results are identical for every value */
-#define ISO_LIMIT_HIST_ROW_CODES 7 /* segment-major histograms: 1 (default) computes each field's
-                                       buckets once for the pairs in which it has the larger
-                                       maximum, 0 computes both buckets in every pair; results
+#define ISO_LIMIT_HIST_ROW_CODES 7 /* segment-major histograms: 1 computes each field's buckets
+                                       once for the pairs in which it has the larger maximum,
+                                       0 (default) computes both buckets in every pair; results
                                        are identical */
 #define ISO_LIMIT_MI_MODE 4 /* ISO_MI_*: how the mutual information of a pair is computed
                                 (default ISO_MI_FP64; the reference-named entry points use

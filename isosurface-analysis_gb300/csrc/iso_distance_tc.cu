@@ -263,9 +263,11 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
                 bapprox = fminf(bapprox, cm);
                 thr = bapprox + tau;
                 const float4 *sP = reinterpret_cast<const float4 *>(sm + SM_P0) + st * TC_POINTS + col0;
+                // padding rows of the last block have no point behind them
+                const int64_t valid = P - b * TC_POINTS - col0;
 #pragma unroll
                 for (int j = 0; j < HALF; ++j) {
-                    if (__uint_as_float(r[j]) <= thr) {
+                    if (__uint_as_float(r[j]) <= thr && j < valid) {
                         const float4 p = sP[j];
                         best = fminf(best, iso_dist2(__fsub_rn(s.x, p.x), __fsub_rn(s.y, p.y), __fsub_rn(s.z, p.z)));
                     }

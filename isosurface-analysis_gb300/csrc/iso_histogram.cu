@@ -1150,7 +1150,9 @@ int iso_run_minmax(iso_ctx *ctx, const float *d_fields, int m, int64_t n, int64_
 
 // Pair tasks ordered in 16-field tiles so concurrently running CTAs share fields
 // in L2.  symmetric: i <= j over one set; otherwise all (i, j) of two sets.
-static void build_tasks(int m, bool symmetric, int2 *out, int *count)
+// Pair tasks in 16 x 16 tiles.  perm (symmetric runs only, may be null):
+// tiles run over perm's positions, and a task (perm[a], perm[b]) has a <= b.
+static void build_tasks(int m, bool symmetric, int2 *out, int *count, const int *perm = nullptr)
 {
     const int T = 16;
     int c = 0;
@@ -1158,7 +1160,7 @@ static void build_tasks(int m, bool symmetric, int2 *out, int *count)
         for (int bj = symmetric ? bi : 0; bj < m; bj += T)
             for (int i = bi; i < bi + T && i < m; ++i)
                 for (int j = bj; j < bj + T && j < m; ++j)
-                    if (!symmetric || j >= i) out[c++] = make_int2(i, j);
+                    if (!symmetric || j >= i) out[c++] = perm ? make_int2(perm[i], perm[j]) : make_int2(i, j);
     *count = c;
 }
 
@@ -1171,7 +1173,23 @@ int iso_run_similarity(iso_ctx *ctx, const float *d_fields_a, const float *d_fie
     const size_t max_tasks = symmetric ? (size_t)m * (m + 1) / 2 : (size_t)m * m;
     std::vector<int2> h_tasks(max_tasks);
     int num_tasks = 0;
-    build_tasks(m, symmetric, h_tasks.data(), &num_tasks);
+    std::vector<int> perm;
+    if (symmetric && ctx->hist_row_codes && bins > WIDE_MAX_BINS && ctx->hist_segment_values > 0 &&
+        n > ctx->hist_segment_values) {
+        // precomputed row buckets: order the fields by their maximum, so that
+        // every task's first field is the one whose codes it reads and a tile
+        // of tasks reads the codes of one 16-field group and the values of
+        // another (the same L2 working set as without codes)
+        std::vector<uint32_t> mm((size_t)2 * m);
+        ISO_CUDA(cudaMemcpyAsync(mm.data(), d_minmax_a, mm.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+        ISO_CUDA(cudaStreamSynchronize(ctx->stream));
+        perm.resize(m);
+        for (int k = 0; k < m; ++k) perm[k] = k;
+        // non-negative maxima: bit order is value order
+        std::stable_sort(perm.begin(), perm.end(), [&](int x, int y) { return mm[2 * x + 1] > mm[2 * y + 1]; });
+    }
+    build_tasks(m, symmetric, h_tasks.data(), &num_tasks, perm.empty() ? nullptr : perm.data());
     if (ctx->mi_mode == ISO_MI_REF32 && !d_joint_dump) {
         // the reference's FP32 MI walks every ordered pair's histogram: keep them all
         void *p;

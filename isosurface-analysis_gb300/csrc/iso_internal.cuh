@@ -115,7 +115,7 @@ struct iso_ctx {
     int mi_mode = ISO_MI_FP64;  // ISO_MI_*: precision and order of the mutual information
     int64_t device_bytes_cap = 0;  // ISO_LIMIT_DEVICE_BYTES (0: none)
     int query_run = 0;             // ISO_LIMIT_QUERY_RUN (0: by volume size)
-    int hist_row_codes = 1;        // ISO_LIMIT_HIST_ROW_CODES
+    int hist_row_codes = 0;        // ISO_LIMIT_HIST_ROW_CODES
     // joint histograms of all ordered pairs kept in BUF_HIST_DUMP by the last
     // ISO_MI_REF32 similarity run (0 = none)
     int joint_m = 0, joint_bins = 0;

@@ -291,3 +291,35 @@ def test_reference_named_entry_256_bins():
             joint_ij, cs, rs = oracle.pair_histogram(a[i], b[j], 256, (mins[i], maxs[i]), (mins[3 + j], maxs[3 + j]))
             assert np.array_equal(cols[i, j], cs) and np.array_equal(rows[i, j], rs)
             assert abs(sim[i, j] - oracle.mi_f32(joint_ij, cs, rs, a.shape[1])) < TOL_REF_HOST
+
+
+def test_row_codes_bit_exact():
+    """Segment-major histograms with precomputed row buckets: the same joint
+    histograms and maps as without them -- symmetric runs (fields ordered by
+    their maximum), cross maps (the coded field is sometimes the pair's second,
+    so the shared histogram is transposed), a field whose minimum is far above
+    the others' (many values near a bucket edge take the divisions) and the
+    reference's FP32 MI over the dumped histograms."""
+    import isosim
+    n = 3 * SEG + 5
+    f = fields_like_df(7, n, seed=71)
+    f[2] += np.float32(0.05)          # a much larger minimum than the others
+    f[5] *= np.float32(2.5)           # the largest maximum
+    g = fields_like_df(7, n, seed=72)[::-1].copy() * np.float32(1.7)
+    out = {}
+    for codes in (0, 1):
+        with isosim.Context(0) as c:
+            c.set_hist_segment_values(SEG)
+            c.set_hist_row_codes(codes)
+            ism, joint = c.similarity_map(f, 256, joint=True)
+            cm = c.cross_map(f, g, 256)
+            c.set_mi_mode(isosim.MI_REF32)
+            ism32 = c.similarity_map(f, 256)
+            cm32 = c.cross_map(f, g, 256)
+            out[codes] = (ism, joint, cm, ism32, cm32)
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
+    for i in range(7):
+        for j in range(7):
+            want, _, _ = oracle.pair_histogram(f[i], f[j], 256)
+            assert np.array_equal(out[1][1][i, j], want), (i, j)
