@@ -16,9 +16,11 @@
 //    so that A.B = |p|^2 - 2 s.p = |s - p|^2 - |s|^2 (the sl*pl products are
 //    dropped).  One tcgen05.mma (M 128, N 128, K 16, f16 in, FP32 out) per
 //    block of points writes a 128 x 128 tile to tensor memory.
-//  * One warp streams the blocks: a bulk copy (TMA) brings a block's B rows and
-//    FP32 points into one of two shared-memory stages, and one thread issues
-//    the block's MMA into one of two accumulators once the copy has landed.
+//  * One warp streams the blocks: bulk copies (TMA) bring a block's B rows and
+//    FP32 points into one of six shared-memory stages (four blocks in
+//    flight), and one thread issues the block's MMA into one of two
+//    accumulators once its copy has landed and the block two before it has
+//    been read back.
 //    Eight warps read the accumulators back (tcgen05.ld): warp w takes the 32
 //    samples of TMEM lane quarter w % 4 and columns 64 (w / 4) .. +63, keeps
 //    the smallest value B of its columns and recomputes the canonical FP32
@@ -58,12 +60,13 @@ constexpr int BRICK_Z = 8, BRICK_Y = 4, BRICK_X = 4;
 // shared memory: A tile, two B stages, two point stages, the halves' minima,
 // barriers and the TMEM slot; padded so that at most two CTAs share an SM
 // (2 x 256 TMEM columns = all 512)
+constexpr int STAGES = 6;                             // operand stages (copies in flight: STAGES - 2)
 constexpr int SM_A = 0;
 constexpr int SM_B0 = 4096;
-constexpr int SM_P0 = SM_B0 + 2 * BLOCK_BYTES;        // 128 float4 per stage
-constexpr int SM_BEST = SM_P0 + 2 * TC_POINTS * 16;   // 128 floats
-constexpr int SM_BAR = SM_BEST + 128 * 4;             // loaded[2], full[2], empty[2], slot
-constexpr int SM_USED = SM_BAR + 64;
+constexpr int SM_P0 = SM_B0 + STAGES * BLOCK_BYTES;        // 128 float4 per stage
+constexpr int SM_BEST = SM_P0 + STAGES * TC_POINTS * 16;   // 128 floats
+constexpr int SM_BAR = SM_BEST + 128 * 4;  // loaded[STAGES], consumed[STAGES], full[2], slot
+constexpr int SM_USED = SM_BAR + (2 * STAGES + 2) * 8 + 16;
 constexpr int SM_ALLOC = 80 * 1024;
 constexpr float SENTINEL_Q = 30000.0f;        // |p|^2 of padding rows: never within tau
 constexpr uint32_t WAIT_LIMIT = 1u << 26;     // polls of one barrier wait before giving up
@@ -144,10 +147,10 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
     extern __shared__ __align__(1024) unsigned char sm[];
     unsigned char *sA = sm + SM_A;
     float *sBest = reinterpret_cast<float *>(sm + SM_BEST);
-    uint64_t *loaded = reinterpret_cast<uint64_t *>(sm + SM_BAR);
-    uint64_t *full = loaded + 2;
-    uint64_t *empty = loaded + 4;
-    uint32_t *slot = reinterpret_cast<uint32_t *>(sm + SM_BAR + 48);
+    uint64_t *loaded = reinterpret_cast<uint64_t *>(sm + SM_BAR);  // stage's copies landed
+    uint64_t *consumed = loaded + STAGES;                            // stage's block read back
+    uint64_t *full = consumed + STAGES;                              // accumulator's MMA done
+    uint32_t *slot = reinterpret_cast<uint32_t *>(full + 2);
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
     const int seg = blockIdx.y;
     const int64_t off = a.sg.offset[seg], P = a.sg.count[seg];
@@ -187,11 +190,12 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
         tau = 2.0f * (2.0f * ((12.0f * 1.1920929e-7f + 9.5367432e-7f) * R * R + 5e-7f) + 6e-7f * R * R);
     }
     if (t == 0) {
-        for (int k = 0; k < 2; ++k) {
+        for (int k = 0; k < STAGES; ++k) {
             mbar_init(&loaded[k], 1);
-            mbar_init(&full[k], 1);
-            mbar_init(&empty[k], READ_WARPS);
+            mbar_init(&consumed[k], READ_WARPS);
         }
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
     }
     if (w == 0) {
         tmem_alloc(slot, TC_COLS);
@@ -212,28 +216,30 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
             const uint64_t adesc = tc_desc(sA);
             const uint32_t idesc = tc_idesc_f16_f32(128, TC_POINTS);
             auto fetch = [&](int64_t b) {
-                const int st = (int)(b & 1);
+                const int st = (int)(b % STAGES);
                 const int64_t cnt = P - b * TC_POINTS < TC_POINTS ? P - b * TC_POINTS : TC_POINTS;
                 mbar_expect_tx(&loaded[st], (uint32_t)(BLOCK_BYTES + cnt * 16));
                 bulk_g2s(sm + SM_B0 + st * BLOCK_BYTES, bsrc + (size_t)b * BLOCK_BYTES, BLOCK_BYTES, &loaded[st]);
                 bulk_g2s(sm + SM_P0 + st * TC_POINTS * 16, a.sg.points + off + b * TC_POINTS, (uint32_t)(cnt * 16),
                          &loaded[st]);
             };
-            fetch(0);
-            if (nblocks > 1) fetch(1);
+            for (int64_t b = 0; b < STAGES && b < nblocks; ++b) fetch(b);
             for (int64_t b = 0; b < nblocks && ok; ++b) {
-                const int st = (int)(b & 1);
-                ok = mbar_wait(&loaded[st], (uint32_t)((b >> 1) & 1), WAIT_LIMIT);
+                const int st = (int)(b % STAGES);
+                ok = mbar_wait(&loaded[st], (uint32_t)((b / STAGES) & 1), WAIT_LIMIT);
                 if (!ok) break;
-                tc_fence_after();
-                tc_mma_f16(tbase + st * TC_POINTS, adesc, tc_desc(sm + SM_B0 + st * BLOCK_BYTES), idesc, 0);
-                tc_commit(&full[st]);
-                // refill the other stage with block b + 1 once block b - 1 has
-                // been read back (its accumulator is then free for MMA b + 1)
-                if (b >= 1 && b + 1 < nblocks) {
-                    ok = mbar_wait(&empty[st ^ 1], (uint32_t)(((b - 1) >> 1) & 1), WAIT_LIMIT);
-                    if (ok) fetch(b + 1);
+                if (b >= 2) {
+                    // block b - 2 read back: its accumulator (b % 2) and its
+                    // stage are free; the stage takes block b - 2 + STAGES
+                    const int64_t done = b - 2;
+                    ok = mbar_wait(&consumed[done % STAGES], (uint32_t)((done / STAGES) & 1), WAIT_LIMIT);
+                    if (!ok) break;
+                    if (done + STAGES < nblocks) fetch(done + STAGES);
                 }
+                tc_fence_after();
+                tc_mma_f16(tbase + (uint32_t)(b & 1) * TC_POINTS, adesc, tc_desc(sm + SM_B0 + st * BLOCK_BYTES), idesc,
+                           0);
+                tc_commit(&full[b & 1]);
             }
         }
         ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
@@ -243,13 +249,14 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
         const int col0 = HALF * (w >> 2);
         const uint32_t lane_addr = tbase + ((uint32_t)(32 * (w & 3)) << 16) + col0;
         for (int64_t b = 0; b < nblocks; ++b) {
-            const int st = (int)(b & 1);
-            ok = __all_sync(0xffffffffu, mbar_wait(&full[st], (uint32_t)((b >> 1) & 1), WAIT_LIMIT));
+            const int acc = (int)(b & 1);
+            const int st = (int)(b % STAGES);
+            ok = __all_sync(0xffffffffu, mbar_wait(&full[acc], (uint32_t)((b >> 1) & 1), WAIT_LIMIT));
             if (!ok) break;
             tc_fence_after();
             uint32_t r[HALF];
-            tmem_ld32_async(lane_addr + st * TC_POINTS, r);
-            tmem_ld32_async(lane_addr + st * TC_POINTS + 32, r + 32);
+            tmem_ld32_async(lane_addr + acc * TC_POINTS, r);
+            tmem_ld32_async(lane_addr + acc * TC_POINTS + 32, r + 32);
             tmem_wait_ld64(r);
             float mm[22];
 #pragma unroll
@@ -275,7 +282,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
             }
             tc_fence_before();
             __syncwarp();
-            if (lane == 0) mbar_arrive(&empty[st]);
+            if (lane == 0) mbar_arrive(&consumed[st]);
         }
         if (w >= 4) sBest[ts] = best;
         named_bar(1, 32 * READ_WARPS);
