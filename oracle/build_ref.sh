@@ -8,6 +8,11 @@
 #                        histogram kernel, run on a GPU by oracle/refgpu.py),
 #                        compiled with nvcc's default flags as the reference's
 #                        CMake build does (no -fmad or precision flags)
+#   ref_mc.cubin         device code of MarchingCube.cu (the reference's own
+#                        marching-cubes kernels) with its lookup tables as
+#                        device arrays (oracle/ref_mc_wrap.cu), nvcc defaults;
+#                        refshim_mc/refshim_texture.h stands in for the
+#                        texture references CUDA 13 no longer has
 # Runs only where the reference tree exists.
 # Usage: oracle/build_ref.sh [reference_root]   (default: $ISO_REFERENCE_ROOT,
 #        else /root/reference)
@@ -29,9 +34,11 @@ nvcc "${FLAGS[@]}" -c "$HERE/ref_approx_wrap.cu" -o "$OUT/ref_approx_wrap.o" &
 nvcc "${FLAGS[@]}" -c "$LIB/isosurfaces_cuda/src/common.cu" -o "$OUT/common.o" &
 nvcc -std=c++17 -cubin "${ARCH[@]}" -w -I"$HERE/refshim" -I"$LIB" \
   "$LIB/isosurfaces_cuda/src/JointHistogram.cu" -o "$OUT/ref_histogram.cubin" &
+nvcc -std=c++17 -cubin "${ARCH[@]}" -w -include "$HERE/refshim_mc/refshim_texture.h" -I"$HERE/refshim" -I"$LIB" \
+  "$HERE/ref_mc_wrap.cu" -o "$OUT/ref_mc.cubin" &
 wait
 nvcc -shared -Xcompiler -fPIC "$OUT/ref_histogram_wrap.o" "$OUT/ref_approx_wrap.o" "$OUT/common.o" -o "$OUT/libisoref.so"
 # where the sources were found, for the CPU tests that read the reference's
 # tables directly (oracle.reference_root())
 echo "$REF" > "$OUT/reference_root.txt"
-echo "built $OUT/libisoref.so and $OUT/ref_histogram.cubin"
+echo "built $OUT/libisoref.so, $OUT/ref_histogram.cubin and $OUT/ref_mc.cubin"

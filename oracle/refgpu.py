@@ -1,5 +1,6 @@
-"""The reference's own GPU histogram kernel, run on this machine's GPU (test
-infrastructure only: a checker, never the engine).
+"""The reference's own GPU kernels -- its joint histogram and its marching
+cubes -- run on this machine's GPU (test infrastructure only: a checker,
+never the engine).  The marching-cubes harness is marching_cubes() below.
 
 oracle/build_ref.sh compiles isosurfaces_cuda/src/JointHistogram.cu from the
 reference's sources, device code only and with nvcc's default flags (as the
@@ -70,11 +71,8 @@ class _Driver:
         # engine) use, so device pointers pass freely between them
         self._check(cu.cuDevicePrimaryCtxRetain(C.byref(ctx), dev), "cuDevicePrimaryCtxRetain")
         self._check(cu.cuCtxSetCurrent(ctx), "cuCtxSetCurrent")
-        mod = C.c_void_p()
-        self._check(cu.cuModuleLoad(C.byref(mod), CUBIN.encode()), "cuModuleLoad")
-        fn = C.c_void_p()
-        self._check(cu.cuModuleGetFunction(C.byref(fn), mod, KERNEL), "cuModuleGetFunction")
-        self.fn = fn
+        self.modules = {}
+        self.fn = self.function(CUBIN, KERNEL)
         cu.cuMemAlloc_v2.argtypes = [C.POINTER(C.c_uint64), C.c_size_t]
         cu.cuMemFree_v2.argtypes = [C.c_uint64]
         cu.cuMemcpyHtoD_v2.argtypes = [C.c_uint64, C.c_void_p, C.c_size_t]
@@ -105,13 +103,34 @@ class _Driver:
     def memset0(self, p, nbytes):
         self._check(self.cu.cuMemsetD8_v2(p, 0, nbytes), "cuMemsetD8")
 
-    def launch(self, grid, block, args):
+    def function(self, cubin, name):
+        """A kernel of a cubin under oracle/_ref/ (each cubin loaded once)."""
+        mod = self.modules.get(cubin)
+        if mod is None:
+            mod = C.c_void_p()
+            self._check(self.cu.cuModuleLoad(C.byref(mod), cubin.encode()), "cuModuleLoad")
+            self.modules[cubin] = mod
+        fn = C.c_void_p()
+        self._check(self.cu.cuModuleGetFunction(C.byref(fn), mod, name), "cuModuleGetFunction")
+        return fn
+
+    def launch(self, grid, block, args, fn=None):
+        """grid: an int (x) or an (x, y) pair; one synchronising launch."""
+        gx, gy = (grid, 1) if isinstance(grid, int) else grid
         ptrs = (C.c_void_p * len(args))(*[C.cast(C.pointer(a), C.c_void_p) for a in args])
-        self._check(self.cu.cuLaunchKernel(self.fn, grid, 1, 1, block, 1, 1, 0, None, ptrs, None), "cuLaunchKernel")
+        self._check(self.cu.cuLaunchKernel(fn if fn is not None else self.fn, gx, gy, 1, block, 1, 1, 0, None,
+                                           ptrs, None), "cuLaunchKernel")
         self._check(self.cu.cuCtxSynchronize(), "cuCtxSynchronize")
 
 
 _DRIVER = None
+
+
+def _driver():
+    global _DRIVER
+    if _DRIVER is None:
+        _DRIVER = _Driver()
+    return _DRIVER
 
 
 def similarity(fields, bins, mins=None, maxs=None, multi=False, block=128):
@@ -121,10 +140,7 @@ def similarity(fields, bins, mins=None, maxs=None, multi=False, block=128):
     the values DistanceField::getInterval gives for non-negative fields).
     Returns (sim [m, m] float32, joint [m*m, bins, bins] uint32,
     col_sums [m*m, bins], row_sums [m*m, bins])."""
-    global _DRIVER
-    if _DRIVER is None:
-        _DRIVER = _Driver()
-    drv = _DRIVER
+    drv = _driver()
     fields = np.ascontiguousarray(fields, dtype=np.float32)
     rows, F = fields.shape
     m = rows // 2 if multi else rows
@@ -198,3 +214,125 @@ def similarity(fields, bins, mins=None, maxs=None, multi=False, block=128):
         for p in bufs:
             drv.free(p)
     return sim.reshape(m, m), joint.reshape(m * m, bins, bins), col.reshape(m * m, bins), row.reshape(m * m, bins)
+
+
+# ---------------------------------------------------------------------------
+# Marching cubes: the reference's classifyVoxel, compactVoxels and
+# generateTriangles (isosurfaces_cuda/src/MarchingCube.cu:84-124,138-149,
+# 189-331), compiled from its sources by oracle/build_ref.sh into
+# oracle/_ref/ref_mc.cubin together with oracle/ref_mc_wrap.cu.
+MC_CUBIN = os.path.join(HERE, "_ref", "ref_mc.cubin")
+MC_THREADS = 128                  # MarchingCube.cpp:591
+MC_NTHREADS = 32                  # isosurfaces_cuda/src/defines.h (NTHREADS)
+MC_CLASSIFY = b"_Z13classifyVoxelPjS_Pf5uint3f"
+MC_COMPACT = b"_Z13compactVoxelsPjS_S_j"
+MC_GENERATE = b"_Z17generateTrianglesP6float4S0_PjS1_Ph5uint3fjj"
+MC_BIND = b"refshim_mc_bind"
+
+
+class Uint3(C.Structure):
+    _fields_ = [("x", C.c_uint), ("y", C.c_uint), ("z", C.c_uint)]
+
+
+def mc_available():
+    return os.path.exists(MC_CUBIN)
+
+
+def _exclusive_scan_u32(a):
+    """thrust::exclusive_scan over uint (thrustWrapper.cu ThrustScanWrapper):
+    unsigned 32-bit sums."""
+    out = np.zeros_like(a)
+    c = np.cumsum(a.astype(np.uint64))
+    out[1:] = (c[:-1] & 0xFFFFFFFF).astype(np.uint32)
+    return out
+
+
+def marching_cubes(volume, dims, iso):
+    """The reference's cudaMarchingCube (MarchingCube.cpp:588-710) for one
+    isovalue, with its own kernels on this GPU.  volume: the flat float32
+    array the reference receives, dims = (dim.x, dim.y, dim.z) with x fastest
+    in the kernels' indexing.  The host steps follow the reference's:
+      * classify on the grid of :594-608 (V/128 blocks of 128, truncated,
+        reshaped to 32768 x (V/128/32768) above 65535 blocks) -- voxels past
+        that grid keep the zeros their buffers start with;
+      * exclusive scans of the occupancy and vertex counts (thrust in the
+        reference; here the same unsigned sums on the host), the active and
+        total counts from the last elements (:624-636, :654-666);
+      * compactVoxels on the classify grid, generateTriangles with NTHREADS
+        threads on ceil(active/NTHREADS) blocks, halved in x and doubled in y
+        while above 65535 (:668-694), maxVerts = V (Isosurface.cpp:263);
+      * the first min(maxVerts, totalVerts) positions sorted and made unique
+        (thrustWrapper.cu:44-56; lexicographic over x, y, z, w).
+    Returns (unique xyz [n, 3] float32 in sorted order, active voxels, total
+    vertices)."""
+    drv = _driver()
+    X, Y, Z = (int(d) for d in dims)
+    V = X * Y * Z
+    vol = np.ascontiguousarray(volume, np.float32).ravel()
+    if vol.size != V:
+        raise ValueError("volume size does not match dims")
+    if V < MC_THREADS:
+        raise ValueError("fewer voxels than one classify block: the reference launches an empty grid")
+    fn = {k: drv.function(MC_CUBIN, k) for k in (MC_CLASSIFY, MC_COMPACT, MC_GENERATE, MC_BIND)}
+    gx, gy = V // MC_THREADS, 1
+    if gx > 65535:
+        gy, gx = gx // 32768, 32768
+    bufs = []
+
+    def alloc(nbytes, zero=True):
+        p = drv.alloc(nbytes)
+        bufs.append(p)
+        if zero:
+            drv.memset0(p, nbytes)
+        return p
+
+    try:
+        d_vol = alloc(V * 4, zero=False)
+        drv.h2d(d_vol, vol)
+        d_verts = alloc(V * 4)
+        d_verts_scan = alloc(V * 4)
+        d_occ = alloc(V * 4)
+        d_occ_scan = alloc(V * 4)
+        d_comp = alloc(V * 4)
+        drv.launch(1, 1, [C.c_uint64(d_vol)], fn[MC_BIND])
+        grid = Uint3(X, Y, Z)
+        drv.launch((gx, gy), MC_THREADS,
+                   [C.c_uint64(d_verts), C.c_uint64(d_occ), C.c_uint64(d_vol), grid, C.c_float(iso)],
+                   fn[MC_CLASSIFY])
+        occ = np.zeros(V, np.uint32)
+        drv.d2h(occ, d_occ)
+        occ_scan = _exclusive_scan_u32(occ)
+        active = int(occ[-1]) + int(occ_scan[-1])
+        if active == 0:
+            return np.zeros((0, 3), np.float32), 0, 0
+        drv.h2d(d_occ_scan, occ_scan)
+        drv.launch((gx, gy), MC_THREADS,
+                   [C.c_uint64(d_comp), C.c_uint64(d_occ), C.c_uint64(d_occ_scan), C.c_uint(V)], fn[MC_COMPACT])
+        verts = np.zeros(V, np.uint32)
+        drv.d2h(verts, d_verts)
+        verts_scan = _exclusive_scan_u32(verts)
+        total = int(verts[-1]) + int(verts_scan[-1])
+        drv.h2d(d_verts_scan, verts_scan)
+        g2x, g2y = -(-active // MC_NTHREADS), 1
+        while g2x > 65535:
+            g2x //= 2
+            g2y *= 2
+        max_verts = V
+        d_pos = alloc(max_verts * 16)
+        d_norm = alloc(max_verts * 16)
+        drv.launch((g2x, g2y), MC_NTHREADS,
+                   [C.c_uint64(d_pos), C.c_uint64(d_norm), C.c_uint64(d_comp), C.c_uint64(d_verts_scan),
+                    C.c_uint64(d_vol), grid, C.c_float(iso), C.c_uint(active), C.c_uint(max_verts)],
+                   fn[MC_GENERATE])
+        n = min(max_verts, total)
+        pos = np.zeros((n, 4), np.float32)
+        if n:
+            drv.d2h(pos, d_pos)
+    finally:
+        for p in bufs:
+            drv.free(p)
+    order = np.lexsort((pos[:, 3], pos[:, 2], pos[:, 1], pos[:, 0]))
+    pos = pos[order]
+    keep = np.ones(len(pos), bool)
+    keep[1:] = np.any(pos[1:] != pos[:-1], axis=1)
+    return np.ascontiguousarray(pos[keep, :3]), active, total
