@@ -13,7 +13,9 @@ step.
 Under torchrun each rank computes its own replica (the pipeline shards by
 volume; no collective on the data path) and rank 0 prints one JSON line.
 --impl reference times the reference's histogram/NMI arithmetic and a CPU
-restatement of its surface and distance stages on the host cores.
+restatement of its surface and distance stages on the host cores; beside that
+value its line carries reference_gpu, the device time of the reference's own
+kernels (compiled from its sources) on the same GPU, over a bounded sample.
 """
 import argparse
 import json
@@ -456,6 +458,82 @@ def cpu_baseline(vol, isos, bins, sample_scale=1.0):
                            "histogram_nmi_per_pair": round(t_pair, 5)}}
 
 
+REF_HIST_FIELDS = 88        # 88^2 ordered pairs x 256^2 bins x 4 B = 2.03 GB: one run under the 2 GiB cap
+REF_HIST_VALUES = 999999    # one 1,000,000-value chunk (JointHistogram.cu:21), its last-chunk path
+
+
+def reference_gpu(vol, isos, bins, k_surfaces=4):
+    """The reference's own kernels on this GPU (its sources compiled into
+    oracle/_ref cubins, driven by oracle/refgpu.py with its host steps), as
+    device time measured with CUDA events around each launch, on a bounded
+    sample scaled to one ISM:
+      * marching cubes of k_surfaces isovalues: classifyVoxel, compactVoxels,
+        generateTriangles (MarchingCube.cu; its thrust scans, vertex sort and
+        host copies not counted);
+      * the LBVH distance field of each of those surfaces over every voxel:
+        Morton, build, box and traversal kernels (BVH.cu; its thrust sort not
+        counted);
+      * one histogram run of calculate_histogram_g: REF_HIST_FIELDS fields of
+        REF_HIST_VALUES values, i.e. 7,744 ordered pairs in one launch (a
+        full run: the reference packs 8,192 pairs of 256 bins into its 2 GiB
+        allocation), scaled to the n^2 ordered pairs and F values of the
+        workload's map.
+    Only what the reference's kernels spend on the GPU counts, so the figure
+    is an upper bound on its throughput.  None when a cubin or the GPU is
+    missing."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    try:
+        import oracle
+        import refgpu
+        if not (refgpu.available() and refgpu.mc_available() and refgpu.bvh_available()):
+            return None
+        refgpu._driver()
+    except Exception as e:  # no GPU or no driver
+        return {"unavailable": "reference kernels not run: %s" % str(e).splitlines()[0][:160]}
+    dims = vol.shape
+    F = int(np.prod(dims))
+    n = len(isos)
+    flat = np.ascontiguousarray(vol, np.float32).ravel()
+    pick = np.linspace(n // 4, 3 * n // 4, k_surfaces).astype(int)
+    t_mc, t_bvh, skipped, points = {}, {}, [], []
+    for k in pick:
+        pts, _, _ = refgpu.marching_cubes(flat, dims, float(isos[k]), timing=t_mc)
+        if len(pts) < 2:
+            skipped.append(int(k))
+            continue
+        try:
+            refgpu.lbvh_distance_field(oracle.normalize_points(pts, dims), dims, timing=t_bvh)
+            points.append(len(pts))
+        except ValueError:
+            skipped.append(int(k))   # a tree the check refuses: not run
+    done = len(points)
+    if done == 0:
+        return {"unavailable": "no sampled surface passed the reference tree check"}
+    rng = np.random.default_rng(7)
+    base = rng.uniform(0.0, 1.0, REF_HIST_VALUES)
+    fields = np.stack([np.abs(base * (1 + 0.02 * q) + 0.1 * rng.standard_normal(REF_HIST_VALUES))
+                       for q in range(REF_HIST_FIELDS)]).astype(np.float32)
+    t_hist = {}
+    refgpu.similarity(fields, bins, timing=t_hist)
+    ms_mc = sum(t_mc.values()) / len(pick)
+    ms_bvh = sum(t_bvh.values()) / done
+    ms_hist = t_hist["calculate_histogram_g"] * (n * n) / REF_HIST_FIELDS ** 2 * F / REF_HIST_VALUES
+    s_ism = (n * (ms_mc + ms_bvh) + ms_hist) / 1e3
+    pairs = n * (n - 1) // 2
+    return {"value": round(pairs / s_ism, 4), "unit": "pairs/s", "kind": "reference kernels, device time",
+            "seconds_per_ism": round(s_ism, 2),
+            "per_unit_ms": {"marching_cubes_per_isovalue": round(ms_mc, 3),
+                            "lbvh_per_surface": round(ms_bvh, 3),
+                            "histogram_run_launch": round(t_hist["calculate_histogram_g"], 3),
+                            "histograms_per_ism": round(ms_hist, 1)},
+            "kernels_ms": {k: round(v, 3) for d in (t_mc, t_bvh, t_hist) for k, v in d.items()},
+            "sample": "%d isovalues (%s) of marching cubes and LBVH fields over all %d voxels%s; one histogram "
+                      "launch of %d fields x %d values (%d ordered pairs) scaled to %d ordered pairs x %d values "
+                      "(extrapolated)" % (done, ",".join(str(int(k)) for k in pick if int(k) not in skipped), F,
+                                          "; skipped %s" % skipped if skipped else "", REF_HIST_FIELDS,
+                                          REF_HIST_VALUES, REF_HIST_FIELDS ** 2, n * n, F)}
+
+
 def run_reference(args):
     """The reference arm: the pipeline's arithmetic on the host cores (the
     CPU restatements under oracle/: the reference's own compiled parts do not
@@ -476,6 +554,7 @@ def run_reference(args):
         vals.append(cpu_baseline(vol, isos, bins, sample_scale=args.ref_scale))
         secs.append(time.perf_counter() - t0)
     v = float(np.median([c["value"] for c in vals]))
+    ref_gpu = None if args.no_ref_gpu else reference_gpu(vol, isos, bins)
     cb = dict(vals[0])
     cb["value"] = round(v, 4)
     line = {"metric": METRIC if args.config == 3 else "ISM pairs/sec", "value": round(v, 4), "unit": "pairs/s",
@@ -487,6 +566,8 @@ def run_reference(args):
             "config": bench_config(args, name, n, bins, world),
             "cpu_baseline": cb,
             "e2e": {"value": round(v, 4), "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if ref_gpu is not None:
+        line["reference_gpu"] = ref_gpu
     print(json.dumps(line), flush=True)
 
 
@@ -781,6 +862,8 @@ def main():
                     help="sample size of each reference-arm step (see cpu_baseline)")
     ap.add_argument("--no-plain", action="store_true", help="skip the brute-force plain-path leg")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes (no autotuner)")
+    ap.add_argument("--no-ref-gpu", action="store_true",
+                    help="reference arm: skip the timing of the reference's own kernels on the GPU")
     ap.add_argument("--hist-codes", type=int, default=None, choices=[0, 1],
                     help="segment-major histograms with (1) or without (0) precomputed row buckets")
     ap.add_argument("--plain-surfaces", type=int, default=2)

@@ -308,7 +308,7 @@ __device__ __forceinline__ Query make_query(float3 s)
 }
 
 // Canonical squared distances from the sample to both child boxes (0 inside):
-// per-axis gap max(lo - s, s - hi, 0), then fma(gz,gz, fma(gy,gy, gx*gx)) --
+// per-axis gap max(lo - s, s - hi, 0), then fma(gz,gz, fma(gx,gx, gy*gy)) --
 // the same expression as the point distance, so a leaf (lo = hi = p) gives
 // exactly its canonical distance.
 __device__ __forceinline__ float2 child_dist2(const Query &q, const float4 &a, const float4 &b, const float4 &c)
@@ -321,7 +321,7 @@ __device__ __forceinline__ float2 child_dist2(const Query &q, const float4 &a, c
     const float2 gx = make_float2(max3f(ux.x, vx.x, 0.0f), max3f(ux.y, vx.y, 0.0f));
     const float2 gy = make_float2(max3f(uy.x, vy.x, 0.0f), max3f(uy.y, vy.y, 0.0f));
     const float2 gz = make_float2(max3f(uz.x, vz.x, 0.0f), max3f(uz.y, vz.y, 0.0f));
-    return __ffma2_rn(gz, gz, __ffma2_rn(gy, gy, __fmul2_rn(gx, gx)));
+    return __ffma2_rn(gz, gz, __ffma2_rn(gx, gx, __fmul2_rn(gy, gy)));
 }
 
 // Query layout: a warp owns an 8 (z) x 4 (y) patch of sample columns and each

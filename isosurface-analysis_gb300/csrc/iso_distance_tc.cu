@@ -20,7 +20,10 @@
 //    FP32 points into one of six shared-memory stages (four blocks in
 //    flight), and one thread issues the block's MMA into one of two
 //    accumulators once its copy has landed and the block two before it has
-//    been read back.
+//    been read back.  Each CTA sweeps the blocks from the one holding the
+//    first point at or beyond its brick's middle in x, wrapping around: with
+//    points ordered by x the samples' running minima settle within the first
+//    blocks, so the later blocks rarely hold a candidate to recheck.
 //    Eight warps read the accumulators back (tcgen05.ld): warp w takes the 32
 //    samples of TMEM lane quarter w % 4 and columns 64 (w / 4) .. +63, keeps
 //    the smallest value B of its columns and recomputes the canonical FP32
@@ -178,12 +181,13 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
     }
     // tau from the largest |s| of the brick (its far corner from the origin)
     // and the surface's largest |p|
-    float tau;
+    float tau, corner_x;
     {
         const int64_t xc = clamp_hi((int64_t)bxi * BRICK_X + BRICK_X - 1, X10 - 1),
                       yc = clamp_hi((int64_t)by * BRICK_Y + BRICK_Y - 1, g.Y10 - 1),
                       zc = clamp_hi((int64_t)bz * BRICK_Z + BRICK_Z - 1, g.Z10 - 1);
         const float3 corner = iso_sample_point(g, (xc * g.Y10 + yc) * g.Z10 + zc);
+        corner_x = corner.x;
         const float smax = sqrtf(corner.x * corner.x + corner.y * corner.y + corner.z * corner.z) * 1.0001f;
         const float R = smax + __uint_as_float(a.pmax[seg]) * 1.0001f;
         // twice (the error bound of two values plus the canonical rounding)
@@ -201,12 +205,31 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
         tmem_alloc(slot, TC_COLS);
         tmem_relinquish();
     }
+    const int nb = (int)((P + TC_POINTS - 1) / TC_POINTS);  // blocks of the surface (< 2^31, checked on the host)
+    if (w == READ_WARPS && lane == 0) {
+        // The sweep over the blocks starts at the block holding the first
+        // point at or beyond the brick's middle in x and wraps around.  The
+        // minimum does not depend on the order; starting near the brick
+        // brings each sample's running minimum close to its final value
+        // within the first blocks when the points are ordered by x (as
+        // marching cubes emits them), so later blocks rarely hold a
+        // candidate.  This lane's sample is the brick's first (ts = 0).
+        const float sx = 0.5f * (s.x + corner_x);
+        int64_t lo = 0, hi = P;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (a.sg.points[off + mid].x < sx) lo = mid + 1;
+            else hi = mid;
+        }
+        const int64_t first = lo / TC_POINTS;
+        slot[1] = (uint32_t)(first < nb ? first : (nb > 0 ? nb - 1 : 0));
+    }
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tbase = *slot;
-    const int64_t nblocks = (P + TC_POINTS - 1) / TC_POINTS;
+    const uint32_t tbase = slot[0];
+    const int start = (int)slot[1];
     const unsigned char *bsrc = a.bops + (size_t)a.block_base[seg] * BLOCK_BYTES;
     bool ok = true;
 
@@ -215,31 +238,41 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
         if (lane == 0) {
             const uint64_t adesc = tc_desc(sA);
             const uint32_t idesc = tc_idesc_f16_f32(128, TC_POINTS);
-            auto fetch = [&](int64_t b) {
-                const int st = (int)(b % STAGES);
-                const int64_t cnt = P - b * TC_POINTS < TC_POINTS ? P - b * TC_POINTS : TC_POINTS;
+            // sweep position i holds block (start + i) mod nb, in stage
+            // i mod STAGES (phase (i / STAGES) & 1) and accumulator i & 1
+            auto fetch = [&](int i, int st) {
+                int blk = start + i;
+                if (blk >= nb) blk -= nb;
+                const int64_t rest = P - (int64_t)blk * TC_POINTS;
+                const int64_t cnt = rest < TC_POINTS ? rest : TC_POINTS;
                 mbar_expect_tx(&loaded[st], (uint32_t)(BLOCK_BYTES + cnt * 16));
-                bulk_g2s(sm + SM_B0 + st * BLOCK_BYTES, bsrc + (size_t)b * BLOCK_BYTES, BLOCK_BYTES, &loaded[st]);
-                bulk_g2s(sm + SM_P0 + st * TC_POINTS * 16, a.sg.points + off + b * TC_POINTS, (uint32_t)(cnt * 16),
-                         &loaded[st]);
+                bulk_g2s(sm + SM_B0 + st * BLOCK_BYTES, bsrc + (size_t)blk * BLOCK_BYTES, BLOCK_BYTES, &loaded[st]);
+                bulk_g2s(sm + SM_P0 + st * TC_POINTS * 16, a.sg.points + off + (int64_t)blk * TC_POINTS,
+                         (uint32_t)(cnt * 16), &loaded[st]);
             };
-            for (int64_t b = 0; b < STAGES && b < nblocks; ++b) fetch(b);
-            for (int64_t b = 0; b < nblocks && ok; ++b) {
-                const int st = (int)(b % STAGES);
-                ok = mbar_wait(&loaded[st], (uint32_t)((b / STAGES) & 1), WAIT_LIMIT);
+            for (int i = 0; i < STAGES && i < nb; ++i) fetch(i, i);
+            int st = 0;
+            uint32_t ph = 0;
+            for (int i = 0; i < nb && ok; ++i) {
+                ok = mbar_wait(&loaded[st], ph, WAIT_LIMIT);
                 if (!ok) break;
-                if (b >= 2) {
-                    // block b - 2 read back: its accumulator (b % 2) and its
-                    // stage are free; the stage takes block b - 2 + STAGES
-                    const int64_t done = b - 2;
-                    ok = mbar_wait(&consumed[done % STAGES], (uint32_t)((done / STAGES) & 1), WAIT_LIMIT);
+                if (i >= 2) {
+                    // position i - 2 read back: its accumulator (i % 2) and
+                    // its stage are free; the stage takes position
+                    // i - 2 + STAGES
+                    const int sd = st >= 2 ? st - 2 : st + STAGES - 2;
+                    ok = mbar_wait(&consumed[sd], st >= 2 ? ph : ph ^ 1u, WAIT_LIMIT);
                     if (!ok) break;
-                    if (done + STAGES < nblocks) fetch(done + STAGES);
+                    if (i - 2 + STAGES < nb) fetch(i - 2 + STAGES, sd);
                 }
                 tc_fence_after();
-                tc_mma_f16(tbase + (uint32_t)(b & 1) * TC_POINTS, adesc, tc_desc(sm + SM_B0 + st * BLOCK_BYTES), idesc,
+                tc_mma_f16(tbase + (uint32_t)(i & 1) * TC_POINTS, adesc, tc_desc(sm + SM_B0 + st * BLOCK_BYTES), idesc,
                            0);
-                tc_commit(&full[b & 1]);
+                tc_commit(&full[i & 1]);
+                if (++st == STAGES) {
+                    st = 0;
+                    ph ^= 1u;
+                }
             }
         }
         ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
@@ -248,10 +281,10 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
         float bapprox = __int_as_float(0x7f800000), thr = bapprox;
         const int col0 = HALF * (w >> 2);
         const uint32_t lane_addr = tbase + ((uint32_t)(32 * (w & 3)) << 16) + col0;
-        for (int64_t b = 0; b < nblocks; ++b) {
-            const int acc = (int)(b & 1);
-            const int st = (int)(b % STAGES);
-            ok = __all_sync(0xffffffffu, mbar_wait(&full[acc], (uint32_t)((b >> 1) & 1), WAIT_LIMIT));
+        int st = 0, blk = start;
+        for (int i = 0; i < nb; ++i) {
+            const int acc = i & 1;
+            ok = __all_sync(0xffffffffu, mbar_wait(&full[acc], (uint32_t)((i >> 1) & 1), WAIT_LIMIT));
             if (!ok) break;
             tc_fence_after();
             uint32_t r[HALF];
@@ -271,7 +304,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
                 thr = bapprox + tau;
                 const float4 *sP = reinterpret_cast<const float4 *>(sm + SM_P0) + st * TC_POINTS + col0;
                 // padding rows of the last block have no point behind them
-                const int64_t valid = P - b * TC_POINTS - col0;
+                const int64_t valid = P - (int64_t)blk * TC_POINTS - col0;
 #pragma unroll
                 for (int j = 0; j < HALF; ++j) {
                     if (__uint_as_float(r[j]) <= thr && j < valid) {
@@ -283,6 +316,8 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&consumed[st]);
+            if (++st == STAGES) st = 0;
+            if (++blk == nb) blk = 0;
         }
         if (w >= 4) sBest[ts] = best;
         named_bar(1, 32 * READ_WARPS);
@@ -305,7 +340,11 @@ int iso_run_distance_tc(iso_ctx *ctx, const IsoSampleGrid &g, const IsoSegments 
     const int64_t X10 = g.F / (g.Y10 * g.Z10);
     // prepared B blocks of every surface
     std::vector<int64_t> base((size_t)m + 1, 0);
-    for (int q = 0; q < m; ++q) base[q + 1] = base[q] + (h_seg_count[q] + TC_POINTS - 1) / TC_POINTS;
+    for (int q = 0; q < m; ++q) {
+        const int64_t nb = (h_seg_count[q] + TC_POINTS - 1) / TC_POINTS;
+        if (nb > 0x7fffffff) return iso_fail(ISO_ERR_ARG, "tensor-core distance: more than 2^31 point blocks");
+        base[q + 1] = base[q] + nb;
+    }
     void *d_bops, *d_base, *d_pmax, *d_err;
     ISO_TRY(iso_buf(ctx, BUF_TC_OPERANDS, (size_t)base[m] * BLOCK_BYTES, &d_bops));
     ISO_TRY(iso_buf(ctx, BUF_STAGING_A, (size_t)(m + 1) * sizeof(int64_t) + (size_t)m * sizeof(uint32_t) + 256,

@@ -149,11 +149,14 @@ bool iso_is_device_ptr(const void *p);
 // exact FP32 primitives
 // ---------------------------------------------------------------------------
 
-// Canonical squared distance: fma(dz,dz, fma(dy,dy, dx*dx)), each step rounded
-// once.  The CPU oracle uses the same expression with libm fmaf.
+// Canonical squared distance: fma(dz,dz, fma(dx,dx, dy*dy)), each step rounded
+// once.  That is how nvcc, with its default contraction, compiles the
+// reference's x2 + y2 + z2 (float3SquaredDistance2_d, isosurfaces_cuda/src/
+// BVH.cu:410-416); its own traversal kernel, run on the GPU, gives the same
+// fields bit for bit.  The CPU oracle uses the same expression with libm fmaf.
 __device__ __forceinline__ float iso_dist2(float dx, float dy, float dz)
 {
-    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+    return __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
 }
 
 // Bucket of isosurfaces_cuda/src/JointHistogram.cu:63-75 with IEEE division.

@@ -385,7 +385,8 @@ static void df_sample(long idx, int X, int Y, int Z, int ds, float s[3])
 }
 
 /* Brute-force FP32 distance field with the engine's canonical rounding:
- * d = s - p per axis, d2 = fma(dz,dz, fma(dy,dy, dx*dx)), DF = sqrt(min d2);
+ * d = s - p per axis, d2 = fma(dz,dz, fma(dx,dx, dy*dy)), DF = sqrt(min d2)
+ * (the reference's x2 + y2 + z2 as nvcc contracts it, BVH.cu:410-416);
  * a single-point surface stores the squared distance, as the reference's
  * traversal does (isosurfaces_cuda/src/BVH.cu:599-611).  pts are normalised. */
 ORC_API void orc_distance_field_f32(const float *pts, long P, int X, int Y, int Z, int ds, float *out)
@@ -397,7 +398,7 @@ ORC_API void orc_distance_field_f32(const float *pts, long P, int X, int Y, int 
         float best = 100000.0f;
         for (long p = 0; p < P; ++p) {
             float dx = s[0] - pts[3 * p], dy = s[1] - pts[3 * p + 1], dz = s[2] - pts[3 * p + 2];
-            float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            float d2 = fmaf(dz, dz, fmaf(dx, dx, dy * dy));
             if (d2 < best) best = d2;
         }
         out[idx] = P == 1 ? best : sqrtf(best);
@@ -473,7 +474,7 @@ static float kd_box_dist(const kd_node *n, const float s[3])
         float m = a > b ? a : b;
         g[d] = m > 0.0f ? m : 0.0f;
     }
-    return fmaf(g[2], g[2], fmaf(g[1], g[1], g[0] * g[0]));
+    return fmaf(g[2], g[2], fmaf(g[0], g[0], g[1] * g[1]));
 }
 
 static float kd_query(const kd_tree *t, const float s[3])
@@ -488,7 +489,7 @@ static float kd_query(const kd_tree *t, const float s[3])
             for (int i = n->start; i < n->start + n->count; ++i) {
                 const float *p = t->pts + 3 * t->idx[i];
                 float dx = s[0] - p[0], dy = s[1] - p[1], dz = s[2] - p[2];
-                float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                float d2 = fmaf(dz, dz, fmaf(dx, dx, dy * dy));
                 if (d2 < best) best = d2;
             }
             continue;
@@ -679,4 +680,152 @@ ORC_API int orc_select_representatives(const float *ism, int m, const int *ids, 
     free(elems);
     free(heap);
     return taken;
+}
+
+/* ------------------------------------------------------------------------
+ * The reference's LBVH construction, restated so that the GPU checker
+ * (oracle/refgpu.py) can verify, before it runs the reference's own BVH
+ * kernels on an input, that the tree they build is a tree: every node but the
+ * root has exactly one parent, every node is reachable from the root, and the
+ * depth stays below the traversal's fixed 64-entry stack
+ * (isosurfaces_cuda/src/BVH.cu:515).  A duplicate-code run takes the
+ * reference's own branch (BVH.cu:202-216), so the check follows the
+ * reference's rules, not the engine's index-augmented ones.
+ * ------------------------------------------------------------------------ */
+
+static int clz32(uint32_t x)
+{
+    int n = 0;
+    if (x == 0) return 32;
+    while (!(x & 0x80000000u)) { x <<= 1; ++n; }
+    return n;
+}
+
+/* morton3D_d and expandBits_d (BVH.cu:86-106) on packed float3 points */
+ORC_API void orc_ref_morton(const float *pts, long n, uint32_t *codes)
+{
+    for (long i = 0; i < n; ++i) {
+        uint32_t c[3];
+        for (int a = 0; a < 3; ++a) {
+            float v = pts[3 * i + a] * 1024.0f;
+            v = v > 0.0f ? v : 0.0f;
+            v = v < 1023.0f ? v : 1023.0f;
+            uint32_t b = (uint32_t)v;
+            b = (b * 0x00010001u) & 0xFF0000FFu;
+            b = (b * 0x00000101u) & 0x0F00F00Fu;
+            b = (b * 0x00000011u) & 0xC30C30C3u;
+            b = (b * 0x00000005u) & 0x49249249u;
+            c[a] = b;
+        }
+        codes[i] = c[0] * 4u + c[1] * 2u + c[2];
+    }
+}
+
+/* delta_d (BVH.cu:170-193): common prefix length, index-extended for equal codes */
+static int ref_delta(const uint32_t *c, long n, long i, long j)
+{
+    if (j >= n || j < 0) return -1;
+    if (c[i] == c[j]) return 32 + clz32((uint32_t)(i ^ j));
+    return clz32(c[i] ^ c[j]);
+}
+
+/* determineRange_d (BVH.cu:195-244) */
+static void ref_range(const uint32_t *c, long n, long idx, long *first, long *last)
+{
+    if (idx == 0) { *first = 0; *last = n - 1; return; }
+    if (idx != n - 1 && c[idx] == c[idx + 1] && c[idx] == c[idx - 1]) {
+        long index = idx;
+        for (;;) {
+            index += 1;
+            if (index >= n - 1) break;
+            if (c[index] != c[index + 1]) break;
+        }
+        *first = idx;
+        *last = index;
+        return;
+    }
+    int dd = ref_delta(c, n, idx, idx + 1) - ref_delta(c, n, idx, idx - 1);
+    long d = dd == 0 ? 0 : (dd < 0 ? -1 : 1);
+    int dmin = ref_delta(c, n, idx, idx - d);
+    long lmax = 2;
+    while (ref_delta(c, n, idx, idx + lmax * d) > dmin) lmax *= 2;
+    long l = 0;
+    for (long t = lmax / 2; t >= 1; t /= 2)
+        if (ref_delta(c, n, idx, idx + (l + t) * d) > dmin) l += t;
+    long j = idx + l * d;
+    if (d < 0) { *first = j; *last = idx; } else { *first = idx; *last = j; }
+}
+
+/* findSplit_d (BVH.cu:122-166) */
+static long ref_split(const uint32_t *c, long first, long last)
+{
+    uint32_t fc = c[first], lc = c[last];
+    if (fc == lc) return first;
+    int common = clz32(fc ^ lc);
+    long split = first, step = last - first;
+    do {
+        step = (step + 1) >> 1;
+        long ns = split + step;
+        if (ns < last && clz32(fc ^ c[ns]) > common) split = ns;
+    } while (step > 1);
+    return split;
+}
+
+/* The reference's tree over n sorted codes (generateInternalNodes_g,
+ * BVH.cu:273-345): child ids of internal node i in left[i], right[i], with
+ * leaves as -(index) - 1 (calcId_d, BVH.cu:23-26).  Returns the tree's depth
+ * (edges on the longest root-to-leaf path), or -1 when it is not a tree (a
+ * node with no or several parents, one unreachable, or a cycle). */
+ORC_API long orc_ref_lbvh(const uint32_t *c, long n, int32_t *left, int32_t *right)
+{
+    if (n < 2) return 0;
+    long ni = n - 1;
+    for (long i = 0; i < ni; ++i) {
+        long f, l;
+        ref_range(c, n, i, &f, &l);
+        long s = ref_split(c, f, l);
+        left[i] = s != f ? (int32_t)s : (int32_t)(-s - 1);
+        right[i] = s + 1 != l ? (int32_t)(s + 1) : (int32_t)(-(s + 1) - 1);
+    }
+    /* parents: internal nodes 0..ni-1, leaves ni..ni+n-1 */
+    int32_t *parents = (int32_t *)calloc((size_t)(ni + n), sizeof(int32_t));
+    long bad = 0;
+    for (long i = 0; i < ni; ++i) {
+        int32_t ch[2] = {left[i], right[i]};
+        for (int k = 0; k < 2; ++k) {
+            long v = ch[k] >= 0 ? ch[k] : ni + (-(long)ch[k] - 1);
+            if (ch[k] == 0 || v >= ni + n) { bad = 1; continue; }
+            parents[v]++;
+        }
+    }
+    for (long v = 1; v < ni + n && !bad; ++v) if (parents[v] != 1) bad = 1;
+    if (parents[0] != 0) bad = 1;
+    long depth = -1;
+    if (!bad) {
+        /* iterative walk from the root; with one parent per node a revisit
+         * cannot happen, so the visit count proves reachability */
+        long *stack = (long *)malloc(sizeof(long) * (size_t)(ni + n));
+        long *dep = (long *)malloc(sizeof(long) * (size_t)(ni + n));
+        long sp = 0, seen = 0, maxd = 0;
+        stack[sp] = 0;
+        dep[sp++] = 0;
+        while (sp > 0) {
+            long v = stack[--sp], dv = dep[sp];
+            ++seen;
+            if (dv > maxd) maxd = dv;
+            if (seen > ni + n) break;
+            if (v < ni) {
+                int32_t ch[2] = {left[v], right[v]};
+                for (int k = 0; k < 2; ++k) {
+                    stack[sp] = ch[k] >= 0 ? ch[k] : ni + (-(long)ch[k] - 1);
+                    dep[sp++] = dv + 1;
+                }
+            }
+        }
+        if (seen == ni + n) depth = maxd;
+        free(stack);
+        free(dep);
+    }
+    free(parents);
+    return depth;
 }

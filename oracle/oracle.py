@@ -55,6 +55,8 @@ def _load_oracle():
         "orc_real_range": (None, [_P, C.c_long, C.c_float, C.c_float, _P, _P]),
         "orc_isovalues": (None, [_P, C.c_long, C.c_float, C.c_float, C.c_int, C.c_int, _P]),
         "orc_select_representatives": (C.c_int, [_P, C.c_int, _P, _P, C.c_int, _P]),
+        "orc_ref_morton": (None, [_P, C.c_long, _P]),
+        "orc_ref_lbvh": (C.c_long, [_P, C.c_long, _P, _P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -264,3 +266,23 @@ def ref_approximation(ref, vol, dims, iso):
     out = np.zeros((max(cap, 1), 3), np.int32)
     n = ref.ref_approximation_cpu(_p(v), iso, X, Y, Z, _p(out), cap)
     return out[:n].copy()
+
+
+def ref_morton(pts):
+    """The reference's 30-bit Morton codes of float32 points (BVH.cu:86-106)."""
+    p = f32(pts).reshape(-1, 3)
+    out = np.zeros(p.shape[0], np.uint32)
+    orc.orc_ref_morton(_p(p), p.shape[0], _p(out))
+    return out
+
+
+def ref_lbvh(sorted_codes):
+    """The reference's tree over sorted Morton codes (BVH.cu:122-345):
+    (left, right, depth) with leaves encoded -(index) - 1; depth -1 when the
+    rules do not give a tree."""
+    c = np.ascontiguousarray(sorted_codes, np.uint32)
+    n = c.size
+    left = np.zeros(max(n - 1, 1), np.int32)
+    right = np.zeros(max(n - 1, 1), np.int32)
+    depth = orc.orc_ref_lbvh(_p(c), n, _p(left), _p(right))
+    return left[:n - 1], right[:n - 1], int(depth)

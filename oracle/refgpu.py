@@ -72,7 +72,10 @@ class _Driver:
         self._check(cu.cuDevicePrimaryCtxRetain(C.byref(ctx), dev), "cuDevicePrimaryCtxRetain")
         self._check(cu.cuCtxSetCurrent(ctx), "cuCtxSetCurrent")
         self.modules = {}
-        self.fn = self.function(CUBIN, KERNEL)
+        self.fn = self.function(CUBIN, KERNEL) if os.path.exists(CUBIN) else None
+        self.ev0, self.ev1 = C.c_void_p(), C.c_void_p()
+        self._check(cu.cuEventCreate(C.byref(self.ev0), 0), "cuEventCreate")
+        self._check(cu.cuEventCreate(C.byref(self.ev1), 0), "cuEventCreate")
         cu.cuMemAlloc_v2.argtypes = [C.POINTER(C.c_uint64), C.c_size_t]
         cu.cuMemFree_v2.argtypes = [C.c_uint64]
         cu.cuMemcpyHtoD_v2.argtypes = [C.c_uint64, C.c_void_p, C.c_size_t]
@@ -80,6 +83,8 @@ class _Driver:
         cu.cuMemsetD8_v2.argtypes = [C.c_uint64, C.c_ubyte, C.c_size_t]
         cu.cuLaunchKernel.argtypes = [C.c_void_p, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_uint,
                                       C.c_uint, C.c_void_p, C.POINTER(C.c_void_p), C.c_void_p]
+        cu.cuEventRecord.argtypes = [C.c_void_p, C.c_void_p]
+        cu.cuEventElapsedTime.argtypes = [C.POINTER(C.c_float), C.c_void_p, C.c_void_p]
 
     def _check(self, rc, what):
         if rc != 0:
@@ -115,12 +120,18 @@ class _Driver:
         return fn
 
     def launch(self, grid, block, args, fn=None):
-        """grid: an int (x) or an (x, y) pair; one synchronising launch."""
+        """grid: an int (x) or an (x, y) pair; one synchronising launch.
+        Returns the launch's device time in ms (CUDA events around it)."""
         gx, gy = (grid, 1) if isinstance(grid, int) else grid
         ptrs = (C.c_void_p * len(args))(*[C.cast(C.pointer(a), C.c_void_p) for a in args])
+        self._check(self.cu.cuEventRecord(self.ev0, None), "cuEventRecord")
         self._check(self.cu.cuLaunchKernel(fn if fn is not None else self.fn, gx, gy, 1, block, 1, 1, 0, None,
                                            ptrs, None), "cuLaunchKernel")
+        self._check(self.cu.cuEventRecord(self.ev1, None), "cuEventRecord")
         self._check(self.cu.cuCtxSynchronize(), "cuCtxSynchronize")
+        ms = C.c_float()
+        self._check(self.cu.cuEventElapsedTime(C.byref(ms), self.ev0, self.ev1), "cuEventElapsedTime")
+        return ms.value
 
 
 _DRIVER = None
@@ -133,13 +144,19 @@ def _driver():
     return _DRIVER
 
 
-def similarity(fields, bins, mins=None, maxs=None, multi=False, block=128):
+def _account(timing, name, ms):
+    if timing is not None:
+        timing[name] = timing.get(name, 0.0) + ms
+
+
+def similarity(fields, bins, mins=None, maxs=None, multi=False, block=128, timing=None):
     """The reference's calculate_histogram_h on the GPU for m fields (2m rows
     in multi mode: the first m against the last m).  fields: [rows, F]
     float32.  mins/maxs: per-row interval (default: each row's min and max,
     the values DistanceField::getInterval gives for non-negative fields).
     Returns (sim [m, m] float32, joint [m*m, bins, bins] uint32,
-    col_sums [m*m, bins], row_sums [m*m, bins])."""
+    col_sums [m*m, bins], row_sums [m*m, bins]).  timing (a dict), if given,
+    accumulates the device ms of each kernel by name."""
     drv = _driver()
     fields = np.ascontiguousarray(fields, dtype=np.float32)
     rows, F = fields.shape
@@ -201,7 +218,7 @@ def similarity(fields, bins, mins=None, maxs=None, multi=False, block=128):
             args = [C.c_uint64(d_fields), C.c_uint64(d_min), C.c_uint64(d_max), C.c_uint64(d_joint),
                     C.c_uint64(d_col), C.c_uint64(d_row), C.c_uint64(d_tasks), C.c_ulong(0), C.c_ulong(off),
                     C.c_uint64(d_sim), ri, di]
-            drv.launch(grid, block, args)
+            _account(timing, "calculate_histogram_g", drv.launch(grid, block, args))
         sim = np.zeros(m * m, np.float32)
         joint = np.zeros(m * m * bins * bins, np.uint32)
         col = np.zeros(m * m * bins, np.uint32)
@@ -247,7 +264,19 @@ def _exclusive_scan_u32(a):
     return out
 
 
-def marching_cubes(volume, dims, iso):
+def mc_generated_voxels(active):
+    """Active voxels the reference's generateTriangles launch covers: NTHREADS
+    per block on ceil(active / NTHREADS) blocks, halved in x (rounding down)
+    and doubled in y while above 65535 (MarchingCube.cpp:668-678), so an odd
+    count loses blocks."""
+    gx, gy = -(-int(active) // MC_NTHREADS), 1
+    while gx > 65535:
+        gx //= 2
+        gy *= 2
+    return min(int(active), gx * gy * MC_NTHREADS)
+
+
+def marching_cubes(volume, dims, iso, with_w=False, timing=None):
     """The reference's cudaMarchingCube (MarchingCube.cpp:588-710) for one
     isovalue, with its own kernels on this GPU.  volume: the flat float32
     array the reference receives, dims = (dim.x, dim.y, dim.z) with x fastest
@@ -264,7 +293,11 @@ def marching_cubes(volume, dims, iso):
       * the first min(maxVerts, totalVerts) positions sorted and made unique
         (thrustWrapper.cu:44-56; lexicographic over x, y, z, w).
     Returns (unique xyz [n, 3] float32 in sorted order, active voxels, total
-    vertices)."""
+    vertices); with with_w, the rows keep their w, which is 1 for every
+    position the kernel wrote and 0 for the zeros of entries it left unwritten
+    (more than maxVerts - 3 triangle vertices, MarchingCube.cu:319) or
+    did not reach (voxels past mc_generated_voxels).  timing (a dict), if
+    given, accumulates the device ms of each of the reference's kernels."""
     drv = _driver()
     X, Y, Z = (int(d) for d in dims)
     V = X * Y * Z
@@ -296,18 +329,19 @@ def marching_cubes(volume, dims, iso):
         d_comp = alloc(V * 4)
         drv.launch(1, 1, [C.c_uint64(d_vol)], fn[MC_BIND])
         grid = Uint3(X, Y, Z)
-        drv.launch((gx, gy), MC_THREADS,
-                   [C.c_uint64(d_verts), C.c_uint64(d_occ), C.c_uint64(d_vol), grid, C.c_float(iso)],
-                   fn[MC_CLASSIFY])
+        _account(timing, "classifyVoxel", drv.launch(
+            (gx, gy), MC_THREADS, [C.c_uint64(d_verts), C.c_uint64(d_occ), C.c_uint64(d_vol), grid, C.c_float(iso)],
+            fn[MC_CLASSIFY]))
         occ = np.zeros(V, np.uint32)
         drv.d2h(occ, d_occ)
         occ_scan = _exclusive_scan_u32(occ)
         active = int(occ[-1]) + int(occ_scan[-1])
         if active == 0:
-            return np.zeros((0, 3), np.float32), 0, 0
+            return np.zeros((0, 4 if with_w else 3), np.float32), 0, 0
         drv.h2d(d_occ_scan, occ_scan)
-        drv.launch((gx, gy), MC_THREADS,
-                   [C.c_uint64(d_comp), C.c_uint64(d_occ), C.c_uint64(d_occ_scan), C.c_uint(V)], fn[MC_COMPACT])
+        _account(timing, "compactVoxels", drv.launch(
+            (gx, gy), MC_THREADS, [C.c_uint64(d_comp), C.c_uint64(d_occ), C.c_uint64(d_occ_scan), C.c_uint(V)],
+            fn[MC_COMPACT]))
         verts = np.zeros(V, np.uint32)
         drv.d2h(verts, d_verts)
         verts_scan = _exclusive_scan_u32(verts)
@@ -320,10 +354,10 @@ def marching_cubes(volume, dims, iso):
         max_verts = V
         d_pos = alloc(max_verts * 16)
         d_norm = alloc(max_verts * 16)
-        drv.launch((g2x, g2y), MC_NTHREADS,
-                   [C.c_uint64(d_pos), C.c_uint64(d_norm), C.c_uint64(d_comp), C.c_uint64(d_verts_scan),
-                    C.c_uint64(d_vol), grid, C.c_float(iso), C.c_uint(active), C.c_uint(max_verts)],
-                   fn[MC_GENERATE])
+        _account(timing, "generateTriangles", drv.launch(
+            (g2x, g2y), MC_NTHREADS,
+            [C.c_uint64(d_pos), C.c_uint64(d_norm), C.c_uint64(d_comp), C.c_uint64(d_verts_scan), C.c_uint64(d_vol),
+             grid, C.c_float(iso), C.c_uint(active), C.c_uint(max_verts)], fn[MC_GENERATE]))
         n = min(max_verts, total)
         pos = np.zeros((n, 4), np.float32)
         if n:
@@ -335,4 +369,136 @@ def marching_cubes(volume, dims, iso):
     pos = pos[order]
     keep = np.ones(len(pos), bool)
     keep[1:] = np.any(pos[1:] != pos[:-1], axis=1)
-    return np.ascontiguousarray(pos[keep, :3]), active, total
+    return np.ascontiguousarray(pos[keep] if with_w else pos[keep, :3]), active, total
+
+
+# ---------------------------------------------------------------------------
+# LBVH distance fields: the reference's calculateMortonCodes_g, initLeaves_g,
+# initNodes_g, generateInternalNodes_g, createBoundingVolumes_g and
+# traverseTree_g (isosurfaces_cuda/src/BVH.cu:108-118,247-368,577-613),
+# compiled from its sources by oracle/build_ref.sh into oracle/_ref/ref_bvh.cubin
+# together with oracle/ref_bvh_wrap.cu.
+BVH_CUBIN = os.path.join(HERE, "_ref", "ref_bvh.cubin")
+BVH_THREADS = 256
+BVH_NUM_SAMPLES = 1500            # runtime/hdr/globals.h (NUM_SAMPLES)
+BVH_MAX_DEPTH = 60                # traverseIterative_d keeps a 64-entry stack (BVH.cu:515)
+BVH_MORTON = b"_Z22calculateMortonCodes_gP6float3iPj"
+BVH_LEAVES = b"_Z12initLeaves_gP8LeafNodeP6float3Pji"
+BVH_NODES = b"_Z11initNodes_gP12InternalNodei"
+BVH_BUILD = b"_Z23generateInternalNodes_gP8LeafNodeP12InternalNodePjii"
+BVH_BOXES = b"_Z23createBoundingVolumes_gP8LeafNodeP12InternalNodePii"
+BVH_TRAVERSE = b"_Z14traverseTree_gP8LeafNodeP12InternalNodePfiiiiiiPjiP6float3b"
+BVH_SIZES = b"refshim_bvh_sizes"
+
+
+def bvh_available():
+    return os.path.exists(BVH_CUBIN)
+
+
+def _blocks(n, threads):
+    return (int(n) + threads - 1) // threads
+
+
+def lbvh_distance_field(points, dims, ds=1, num_samples=BVH_NUM_SAMPLES, timing=None):
+    """The reference's generateHierarchy_h (BVH.cu:815-875) for one surface,
+    with its own kernels on this GPU.  points: [P, 3] float32, already divided
+    by the largest dimension as generateHierarchy_W does (funcs.cpp:150-160);
+    dims = the volume's (dimX, dimY, dimZ).  Returns the float32 field of
+    (dimX/ds)(dimY/ds)(dimZ/ds) samples in the reference's order.
+
+    The reference's kernels are run only on a tree that has been checked
+    first: the Morton codes from its kernel must equal the restatement's
+    (oracle.ref_morton); the codes are sorted on the host by a stable sort (as
+    thrust's radix sort_by_key orders equal keys); the restated tree
+    (oracle.ref_lbvh) must be a tree no deeper than BVH_MAX_DEPTH; and the
+    child ids the reference's build kernel writes must equal the restated
+    ones before the box and traversal kernels run.  The seeds of the
+    traversal are the reference's (traverse_h, BVH.cu:640-644: unsigned
+    32-bit i * P / numSamples).  timing (a dict), if given, accumulates the
+    device ms of each of the reference's kernels."""
+    import oracle
+    drv = _driver()
+    pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    n = pts.shape[0]
+    if n < 2:
+        raise ValueError("fewer than two points: the reference launches empty grids")
+    X, Y, Z = (int(d) for d in dims)
+    size = (X // ds) * (Y // ds) * (Z // ds)
+    fn = {k: drv.function(BVH_CUBIN, k) for k in
+          (BVH_MORTON, BVH_LEAVES, BVH_NODES, BVH_BUILD, BVH_BOXES, BVH_TRAVERSE, BVH_SIZES)}
+    bufs = []
+
+    def alloc(nbytes, zero=True):
+        p = drv.alloc(nbytes)
+        bufs.append(p)
+        if zero:
+            drv.memset0(p, nbytes)
+        return p
+
+    try:
+        d_info = alloc(64)
+        drv.launch(1, 1, [C.c_uint64(d_info)], fn[BVH_SIZES])
+        info = np.zeros(16, np.int32)
+        drv.d2h(info, d_info)
+        leaf_sz, node_sz, f3_sz, off_l, off_r = (int(v) for v in info[:5])
+        if f3_sz != 12:
+            raise RuntimeError("unexpected float3 size %d" % f3_sz)
+        d_pts = alloc(n * 12, zero=False)
+        d_codes = alloc(n * 4)
+        drv.h2d(d_pts, pts)
+        _account(timing, "calculateMortonCodes_g", drv.launch(
+            _blocks(n, BVH_THREADS), BVH_THREADS, [C.c_uint64(d_pts), C.c_int(n), C.c_uint64(d_codes)],
+            fn[BVH_MORTON]))
+        codes = np.zeros(n, np.uint32)
+        drv.d2h(codes, d_codes)
+        if not np.array_equal(codes, oracle.ref_morton(pts)):
+            raise RuntimeError("the reference's Morton codes differ from the restatement: tree not built")
+        order = np.argsort(codes, kind="stable")
+        codes = np.ascontiguousarray(codes[order])
+        drv.h2d(d_codes, codes)
+        drv.h2d(d_pts, np.ascontiguousarray(pts[order]))
+        left, right, depth = oracle.ref_lbvh(codes)
+        if depth < 0 or depth > BVH_MAX_DEPTH:
+            raise ValueError("the reference's rules give no tree of depth <= %d here (%d): not run"
+                             % (BVH_MAX_DEPTH, depth))
+        d_leaves = alloc(n * leaf_sz)
+        d_nodes = alloc((n - 1) * node_sz)
+        _account(timing, "initLeaves_g", drv.launch(
+            _blocks(n, BVH_THREADS), BVH_THREADS,
+            [C.c_uint64(d_leaves), C.c_uint64(d_pts), C.c_uint64(d_codes), C.c_int(n)], fn[BVH_LEAVES]))
+        _account(timing, "initNodes_g", drv.launch(
+            _blocks(n - 1, BVH_THREADS), BVH_THREADS, [C.c_uint64(d_nodes), C.c_int(n - 1)], fn[BVH_NODES]))
+        _account(timing, "generateInternalNodes_g", drv.launch(
+            _blocks(n - 1, BVH_THREADS), BVH_THREADS,
+            [C.c_uint64(d_leaves), C.c_uint64(d_nodes), C.c_uint64(d_codes), C.c_int(n), C.c_int(n - 1)],
+            fn[BVH_BUILD]))
+        raw = np.zeros((n - 1) * node_sz, np.uint8)
+        drv.d2h(raw, d_nodes)
+        raw = raw.reshape(n - 1, node_sz)
+        gl = raw[:, off_l:off_l + 4].copy().view(np.int32).ravel()
+        gr = raw[:, off_r:off_r + 4].copy().view(np.int32).ravel()
+        if not (np.array_equal(gl, left) and np.array_equal(gr, right)):
+            raise RuntimeError("the reference's build kernel made another tree than the checked one: not traversed")
+        d_block = alloc(n * 4)
+        _account(timing, "createBoundingVolumes_g", drv.launch(
+            _blocks(n, BVH_THREADS), BVH_THREADS,
+            [C.c_uint64(d_leaves), C.c_uint64(d_nodes), C.c_uint64(d_block), C.c_int(n)], fn[BVH_BOXES]))
+        ns = min(int(num_samples), n)
+        ids = ((np.arange(ns, dtype=np.uint64) * np.uint64(n)) & np.uint64(0xFFFFFFFF)) // np.uint64(ns)
+        ids = ids.astype(np.uint32)
+        if ids.max() >= n:
+            raise RuntimeError("seed index out of range")
+        d_ids = alloc(ns * 4)
+        drv.h2d(d_ids, ids)
+        d_dist = alloc(size * 4)
+        _account(timing, "traverseTree_g", drv.launch(
+            _blocks(size, BVH_THREADS), BVH_THREADS,
+            [C.c_uint64(d_leaves), C.c_uint64(d_nodes), C.c_uint64(d_dist), C.c_int(size), C.c_int(X), C.c_int(Y),
+             C.c_int(Z), C.c_int(ns), C.c_int(n), C.c_uint64(d_ids), C.c_int(ds), C.c_uint64(0), C.c_bool(False)],
+            fn[BVH_TRAVERSE]))
+        out = np.zeros(size, np.float32)
+        drv.d2h(out, d_dist)
+    finally:
+        for p in bufs:
+            drv.free(p)
+    return out
