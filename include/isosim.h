@@ -414,9 +414,9 @@ ISO_API void iso_server_destroy(iso_server *s);
  * Limits: m <= ISO_NOALLOC_MAX_FIELDS and n <= ISO_NOALLOC_MAX_VALUES (larger
  * m or n return ISO_ERR_CAPACITY); bins even in [2, 256], a bad stride or
  * alignment, or host pointers return ISO_ERR_ARG.  The first call on a
- * device looks up the array's device address and fills a lookup table, so
- * make it before any stream capture.  All calls share the array: calls that
- * overlap on the GPU race. */
+ * device looks up the array's device address and fills a lookup table.  Every
+ * call synchronises its stream, so no call can be captured into a CUDA graph.
+ * All calls share the array: calls that overlap on the GPU race. */
 ISO_API int iso_similarity_map_noalloc(const float *d_fields, int m, int64_t n, int64_t stride, int bins,
                                        float *d_ism_out, void *stream);
 
