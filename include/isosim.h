@@ -303,8 +303,12 @@ typedef struct iso_int3 { int32_t x, y, z; } iso_int3;
  * h_simMap (simMapSize x simMapSize), per-ordered-pair column and row sums
  * (numFields^2 * histogramSize each).  h_jointHist is left untouched, as the
  * reference leaves it (its copy-back is commented out, :397).  The map is the
- * reference's FP32 MI, bit for bit (ISO_MI_REF32).  Runs on the calling
- * thread's current CUDA device, through a process-wide context per device. */
+ * reference's FP32 MI, bit for bit (ISO_MI_REF32).  Values above their
+ * field's maxValue count in the last bucket, as in the reference; an interval
+ * whose minValue lies above one of its field's values is refused (nothing is
+ * written; iso_last_error names the field), since the reference would index
+ * below its histogram there.  Runs on the calling thread's current CUDA
+ * device, through a process-wide context per device. */
 ISO_API void calculate_histogram_h(float **distanceFields, float *minValues, float *maxValues, const int fieldSize,
                                    const unsigned long numFields, const unsigned long histogramSize,
                                    unsigned int *h_jointHist, unsigned int *h_colSums, unsigned int *h_rowSums,

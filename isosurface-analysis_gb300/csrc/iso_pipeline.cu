@@ -331,9 +331,11 @@ static int similarity_impl(iso_ctx *ctx, const float *const *field_ptrs, const f
                                    cudaMemcpyDefault, ctx->stream));
     }
     if (mins && maxs) {
-        // caller-supplied intervals (the reference's getInterval values) must
-        // contain the data: the reference would index below its histogram
-        // otherwise (JointHistogram.cu:69-73)
+        // caller-supplied intervals (the reference's getInterval values): a
+        // value above its field's maximum counts in the last bucket, as the
+        // reference clamps it (JointHistogram.cu:74); a value below the
+        // minimum is refused, since the reference would index below its
+        // histogram there (JointHistogram.cu:69-73)
         ISO_TRY(iso_run_minmax(ctx, f, nf, n, stride, (uint32_t *)d_mm));
         std::vector<uint32_t> mm((size_t)2 * nf);
         std::vector<float> hmin(nf), hmax(nf);
@@ -345,9 +347,10 @@ static int similarity_impl(iso_ctx *ctx, const float *const *field_ptrs, const f
             float lo, hi;
             memcpy(&lo, &mm[2 * k], sizeof lo);
             memcpy(&hi, &mm[2 * k + 1], sizeof hi);
-            if (!(hmin[k] <= lo) || !(hmax[k] >= hi))
-                return iso_fail(ISO_ERR_ARG, "field %d: interval [%g, %g] does not contain its values [%g, %g]", k,
-                                hmin[k], hmax[k], lo, hi);
+            if (!(hmin[k] <= lo) || !(hmax[k] >= hmin[k]))
+                return iso_fail(ISO_ERR_ARG, "field %d: interval [%g, %g] is empty or above its smallest value %g", k,
+                                hmin[k], hmax[k], lo);
+            (void)hi;
         }
         void *d_tmp;
         ISO_TRY(iso_buf(ctx, BUF_STAGING_B, (size_t)2 * nf * sizeof(float), &d_tmp));

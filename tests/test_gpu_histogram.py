@@ -323,3 +323,41 @@ def test_row_codes_bit_exact():
         for j in range(7):
             want, _, _ = oracle.pair_histogram(f[i], f[j], 256)
             assert np.array_equal(out[1][1][i, j], want), (i, j)
+
+
+@pytest.mark.parametrize("n", [300001, 2500003])
+def test_values_above_caller_maxima_256_bins(n):
+    """Caller-supplied maxima below the fields' largest values (the
+    reference-named entry takes its intervals from its caller): those values
+    count in the last bucket, as the reference clamps them, in the fused
+    kernel (300,001 values) and the segment-major kernels (2,500,003); column
+    and row sums bit-exact against the oracle, the map within the
+    host-evaluation bound."""
+    import isosim
+    m = 4
+    fields = list(fields_like_df(m, n, seed=n % 1000))
+    mins, maxs = [], []
+    for f in fields:
+        lo, hi = oracle.field_interval(f)
+        mins.append(float(lo))
+        maxs.append(float(np.float32(hi - 0.2 * (hi - lo))))
+    sim, cols, rows = isosim.calculate_histogram_h(fields, mins, maxs, 256)
+    above = 0
+    for i in range(m):
+        for j in range(m):
+            joint, cs, rs = oracle.pair_histogram(fields[i], fields[j], 256, (mins[i], maxs[i]), (mins[j], maxs[j]))
+            assert np.array_equal(cols[i, j], cs) and np.array_equal(rows[i, j], rs), (i, j)
+            assert abs(sim[i, j] - oracle.mi_f32(joint, cs, rs, n)) < TOL_REF_HOST
+        above += int(np.count_nonzero(fields[i] > max(maxs)))
+    assert above > 0
+
+
+def test_values_below_caller_minimum_refused():
+    """A caller-supplied minimum above one of its field's values is refused
+    (the reference would index below its histogram)."""
+    import isosim
+    fields = list(fields_like_df(3, 50021, seed=5))
+    mins = [float(np.float32(oracle.field_interval(f)[0] + 0.05)) for f in fields]
+    maxs = [float(oracle.field_interval(f)[1]) for f in fields]
+    with pytest.raises(isosim.IsoError, match="above its smallest value"):
+        isosim.calculate_histogram_h(fields, mins, maxs, 256)
