@@ -309,6 +309,8 @@ def run_ours(args):
         "roofline": roofline,
         "clocks": clocks,
     }
+    if rank == 0 and not args.no_ref32:
+        line["mi_ref32"] = ref32_leg(ctx, step, d_vol, ism_dev, flush, stream, m, pairs, args.steps)
     if rank == 0 and not args.no_plain:
         line["plain"] = plain_leg(ctx, vol, isos, sstats, stage, pairs, value, args.plain_surfaces)
     if rank == 0 and not args.no_cpu:
@@ -348,6 +350,40 @@ def histogram_traffic():
     if vals.get("source_sha256") != sha:
         return None, "ncu summary was captured on another histogram source"
     return float(vals["traffic_bytes_per_ism"]), "ncu capture (%s)" % os.path.relpath(TRAFFIC_PROFILE, ROOT)
+
+
+def ref32_leg(ctx, step, d_vol, ism_dev, flush, stream, m, pairs, steps):
+    """The same ISM with the reference's own FP32 MI evaluation (ISO_MI_REF32:
+    every ordered pair's joint histogram kept and evaluated in the reference's
+    order and contraction, bit for bit its kernel's map), timed like the
+    headline (device-resident, L2 flushed, CUDA events), and its largest
+    difference from the FP64 map of the timed steps."""
+    import torch
+
+    import isosim
+    fp64 = ism_dev[:m * m].cpu().numpy().reshape(m, m).copy()
+    ctx.set_mi_mode(isosim.MI_REF32)
+    try:
+        step(d_vol, ism_dev)
+        ms = 0.0
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            _, _, _, timing = step(d_vol, ism_dev)
+            ev1.record(stream)
+            ev1.synchronize()
+            ms += ev0.elapsed_time(ev1)
+        ms /= steps
+        ref32 = ism_dev[:m * m].cpu().numpy().reshape(m, m)
+    finally:
+        ctx.set_mi_mode(isosim.MI_FP64)
+    return {"value": round(pairs / (ms / 1e3), 2), "unit": "pairs/s", "ms_per_ism": round(ms, 3),
+            "histograms_nmi_ms": round(timing.histogram_ms, 3),
+            "max_abs_diff_vs_fp64": float(np.abs(ref32 - fp64).max()),
+            "note": "the reference's FP32 MI evaluation per ordered pair, bit-identical to its own kernel"}
 
 
 def plain_leg(ctx, vol, isos, sstats, stage, pairs, value, k_surfaces):
@@ -817,6 +853,13 @@ def run_case(case, hist_seg=None, hist_codes=None):
         vol, isos, bins = synth.config3(size=160, n=32)
         for _ in range(2):
             ctx.ism(vol.ravel(), (160, 160, 160), isos, bins=bins)
+    elif case == "ism-ref32":
+        # the 256^3 benchmark ISM with the reference's own FP32 MI (every
+        # ordered pair's joint histogram kept, then mi_ref32_kernel)
+        vol, isos, bins = synth.config3()
+        ctx.set_mi_mode(isosim.MI_REF32)
+        for _ in range(2):
+            ctx.ism(vol.ravel(), (256, 256, 256), isos, bins=bins)
     elif case == "tc-small":
         # one surface of the 128^3 k^-3 field through the tensor-core distance
         # kernel (and the LBVH for comparison)
@@ -862,6 +905,8 @@ def main():
                     help="sample size of each reference-arm step (see cpu_baseline)")
     ap.add_argument("--no-plain", action="store_true", help="skip the brute-force plain-path leg")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes (no autotuner)")
+    ap.add_argument("--no-ref32", action="store_true",
+                    help="skip the timing of the reference-exact FP32 MI mode (ISO_MI_REF32)")
     ap.add_argument("--no-ref-gpu", action="store_true",
                     help="reference arm: skip the timing of the reference's own kernels on the GPU")
     ap.add_argument("--hist-codes", type=int, default=None, choices=[0, 1],
@@ -869,7 +914,7 @@ def main():
     ap.add_argument("--plain-surfaces", type=int, default=2)
     ap.add_argument("--serving-requests", type=int, default=24,
                     help="requests of the serving leg in the default line (0: none)")
-    ap.add_argument("--case", default=None, choices=["hist-small", "pipe-small", "ism-128", "tc-small", "seg-small"],
+    ap.add_argument("--case", default=None, choices=["hist-small", "pipe-small", "ism-128", "tc-small", "seg-small", "ism-ref32"],
                     help="run a small fixed case twice and exit (profiling target)")
     ap.add_argument("--mode", default="single", choices=["single", "serving", "multi"])
     ap.add_argument("--requests", type=int, default=40)

@@ -1196,12 +1196,18 @@ int iso_run_similarity(iso_ctx *ctx, const float *d_fields_a, const float *d_fie
         ISO_TRY(iso_buf(ctx, BUF_HIST_DUMP, (size_t)m * m * bins * bins * sizeof(uint32_t), &p));
         d_joint_dump = (uint32_t *)p;
     }
+    if (ctx->mi_mode == ISO_MI_REF32 && !d_colrow_dump) {
+        // and its marginals (exact integers: their summation order is free)
+        void *p;
+        ISO_TRY(iso_buf(ctx, BUF_REF32_SUMS, (size_t)2 * m * m * bins * sizeof(uint32_t), &p));
+        d_colrow_dump = (uint32_t *)p;
+    }
     ISO_TRY(iso_run_similarity_tasks(ctx, d_fields_a, symmetric ? d_fields_a : d_fields_b, m, n, stride, bins,
                                      d_minmax_a, symmetric ? d_minmax_a : d_minmax_b, d_ism, h_tasks.data(), num_tasks,
                                      symmetric, d_joint_dump, d_colrow_dump));
     ctx->joint_m = 0;
     if (ctx->mi_mode == ISO_MI_REF32) {
-        ISO_TRY(iso_run_mi_ref32(ctx, d_joint_dump, m, bins, n, d_ism));
+        ISO_TRY(iso_run_mi_ref32(ctx, d_joint_dump, d_colrow_dump, m, bins, n, d_ism));
         if (d_joint_dump == (uint32_t *)ctx->buf[BUF_HIST_DUMP]) {
             ctx->joint_m = m;
             ctx->joint_bins = bins;

@@ -91,6 +91,8 @@ enum IsoBuf {
     BUF_SURF_BLOCK_COUNTS,  // marching cubes: per block and isovalue, the vertex versions it counted
     BUF_ROW_CODES,          // segment-major histograms: per field and value, its precomputed row bucket
     BUF_TC_OPERANDS,        // tensor-core distance: every surface's points as MMA operand rows
+    BUF_REF32_SUMS,         // reference FP32 MI: column and row sums of every ordered pair
+    BUF_LOGF_TABLE,         // reference FP32 MI: logf of every count below 65536
     BUF_COUNT_
 };
 
@@ -227,7 +229,10 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
 int iso_run_minmax(iso_ctx *ctx, const float *d_fields, int m, int64_t n, int64_t stride, uint32_t *d_minmax);
 // The reference's FP32 MI (calculateMutualInformation, summation order and
 // contraction included) of all m*m ordered pairs whose joint histograms are at
-// d_joint (pair i*m + j at d_joint + (i*m + j)*bins*bins), into d_ism[i*m + j].
-int iso_run_mi_ref32(iso_ctx *ctx, const uint32_t *d_joint, int m, int bins, int64_t n, float *d_ism);
+// d_joint (pair i*m + j at d_joint + (i*m + j)*bins*bins) and whose column and
+// row sums are at d_colrow ([2][m*m*bins], as the histogram kernels dump
+// them), into d_ism[i*m + j].
+int iso_run_mi_ref32(iso_ctx *ctx, const uint32_t *d_joint, const uint32_t *d_colrow, int m, int bins, int64_t n,
+                     float *d_ism);
 
 constexpr int ISO_MAX_ISOVALUES = 4096;

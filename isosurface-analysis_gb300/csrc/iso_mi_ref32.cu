@@ -17,76 +17,94 @@
 // forbids contraction.
 //
 // Layout: joint histograms of all m*m ordered pairs, pair q = i*m + j at
-// joint + q*bins*bins, row = bucket of field i (the histogram kernels' dump).
-// One warp walks 32 pairs, one lane per pair: it stages 32 consecutive bins of
-// each of its pairs in shared memory with coalesced loads (adding them into
-// per-pair column sums there), then each lane continues its pair's serial sums
-// over the staged bins.  Row sums are formed by the walking lane at each row
-// end; column sums are summed once the walk is done.  The order of every
-// summation chain is the reference's.
+// joint + q*bins*bins, row = bucket of field i (the histogram kernels' dump),
+// and their column and row sums (colrow: [2][m*m*bins]; exact integers, so
+// the histogram kernels' sums are the reference's).  One warp walks 32
+// pairs, one lane per pair: it stages 32 consecutive bins of each of its
+// pairs in shared memory with coalesced loads, then each lane continues its
+// pair's serial sum over the staged bins.  The row entropy is the sum over the
+// row sums in row order (the reference adds each at its row's end), the column
+// entropy over the column sums in column order.  The logarithm of a count
+// below 65536 is read from a table that logf_table_kernel fills with the
+// device's own logf, so the serial chains carry only the fused
+// multiply-subtract.  The order of every summation chain is the reference's.
 #include "iso_internal.cuh"
 
 namespace {
 
-constexpr int R32_PAIRS = 32;  // ordered pairs per CTA (one warp, one lane per pair)
-constexpr int R32_TILE = 32;   // bins of each pair staged per step
+constexpr int R32_PAIRS = 32;        // ordered pairs per CTA (one warp, one lane per pair)
+constexpr int R32_TILE = 32;         // bins of each pair staged per step
+constexpr int R32_LOG_TABLE = 65536; // counts whose logarithm is tabulated
 
-// The reference's per-bin term h -= c * logf(c) for a nonzero count.  Kept as
-// one expression so that the compiler fuses the product into the subtraction
-// exactly as it does in the reference's kernel.
-__device__ __forceinline__ float entropy_step(float h, uint32_t count)
+__global__ void logf_table_kernel(float *t)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < R32_LOG_TABLE) t[c] = logf((float)c);
+}
+
+__device__ __forceinline__ float log_count(const float *__restrict__ tab, uint32_t c)
+{
+    return c < (uint32_t)R32_LOG_TABLE ? __ldg(tab + c) : logf((float)c);
+}
+
+// The reference's per-bin term h -= c * logf(c) for a nonzero count, with
+// lg = logf(c).  Kept as one expression so that the compiler fuses the
+// product into the subtraction exactly as it does in the reference's kernel.
+__device__ __forceinline__ float entropy_step(float h, uint32_t count, float lg)
 {
     float c = (float)count;
-    h -= c * logf(c);
+    h -= c * lg;
     return h;
 }
 
-__global__ void __launch_bounds__(R32_PAIRS) mi_ref32_kernel(const uint32_t *__restrict__ joint, int64_t num_pairs,
-                                                            int bins, float num_values, float *__restrict__ ism)
+__global__ void __launch_bounds__(R32_PAIRS) mi_ref32_kernel(const uint32_t *__restrict__ joint,
+                                                            const uint32_t *__restrict__ colrow, int64_t num_pairs,
+                                                            int bins, float num_values,
+                                                            const float *__restrict__ logtab, float *__restrict__ ism)
 {
-    extern __shared__ uint32_t smem[];
-    uint32_t *tile = smem;                                     // [R32_PAIRS][R32_TILE + 1]
-    uint32_t *colsum = smem + R32_PAIRS * (R32_TILE + 1);      // [R32_PAIRS][bins]
+    __shared__ uint32_t tile[R32_PAIRS * (R32_TILE + 1)];
     const int lane = threadIdx.x;
     const int64_t first = (int64_t)blockIdx.x * R32_PAIRS;
     const int64_t hist = (int64_t)bins * bins;
-    for (int k = lane; k < R32_PAIRS * bins; k += R32_PAIRS) colsum[k] = 0;
-    __syncwarp();
 
-    float hXY = 0.0f, hY = 0.0f;
-    uint32_t row_sum = 0;
-    int col = 0;
+    float hXY = 0.0f;
     for (int64_t k0 = 0; k0 < hist; k0 += R32_TILE) {
         // stage bins k0 .. k0+31 of every pair of this CTA (128 B per pair)
         const int64_t k = k0 + lane;
-        const int kcol = (int)(k % bins);
-#pragma unroll 4
+#pragma unroll 8
         for (int p = 0; p < R32_PAIRS; ++p) {
             uint32_t v = 0;
             if (first + p < num_pairs && k < hist) v = __ldcs(joint + (first + p) * hist + k);
             tile[p * (R32_TILE + 1) + lane] = v;
-            if (v) atomicAdd(&colsum[p * bins + kcol], v);
         }
         __syncwarp();
         // this lane's pair: the reference's row-major walk over the staged bins
-        const int steps = hist - k0 < R32_TILE ? (int)(hist - k0) : R32_TILE;
-        for (int s = 0; s < steps; ++s) {
-            const uint32_t v = tile[lane * (R32_TILE + 1) + s];
-            if (v > 0) hXY = entropy_step(hXY, v);
-            row_sum += v;
-            if (++col == bins) {
-                if (row_sum > 0) hY = entropy_step(hY, row_sum);
-                row_sum = 0;
-                col = 0;
+        const uint32_t *own = tile + lane * (R32_TILE + 1);
+        if (hist - k0 >= R32_TILE) {
+#pragma unroll
+            for (int s = 0; s < R32_TILE; ++s) {
+                const uint32_t v = own[s];
+                if (v > 0) hXY = entropy_step(hXY, v, log_count(logtab, v));
+            }
+        } else {
+            for (int s = 0; s < (int)(hist - k0); ++s) {
+                const uint32_t v = own[s];
+                if (v > 0) hXY = entropy_step(hXY, v, log_count(logtab, v));
             }
         }
         __syncwarp();
     }
     if (first + lane >= num_pairs) return;
-    float hX = 0.0f;
+    const uint32_t *cs = colrow + (first + lane) * bins;
+    const uint32_t *rs = colrow + num_pairs * bins + (first + lane) * bins;
+    float hX = 0.0f, hY = 0.0f;
     for (int c = 0; c < bins; ++c) {
-        const uint32_t v = colsum[lane * bins + c];
-        if (v > 0) hX = entropy_step(hX, v);
+        const uint32_t v = __ldg(cs + c);
+        if (v > 0) hX = entropy_step(hX, v, log_count(logtab, v));
+    }
+    for (int r = 0; r < bins; ++r) {
+        const uint32_t v = __ldg(rs + r);
+        if (v > 0) hY = entropy_step(hY, v, log_count(logtab, v));
     }
     // JointHistogram.cu:53-59, operation for operation
     hXY = hXY / num_values + logf(num_values);
@@ -100,17 +118,23 @@ __global__ void __launch_bounds__(R32_PAIRS) mi_ref32_kernel(const uint32_t *__r
 }  // namespace
 
 // Reference-order FP32 MI of all m*m ordered pairs whose joint histograms are
-// at d_joint (pair i*m + j, row = bucket of field i); n = values per field.
-int iso_run_mi_ref32(iso_ctx *ctx, const uint32_t *d_joint, int m, int bins, int64_t n, float *d_ism)
+// at d_joint (pair i*m + j, row = bucket of field i) and column and row sums at
+// d_colrow; n = values per field.
+int iso_run_mi_ref32(iso_ctx *ctx, const uint32_t *d_joint, const uint32_t *d_colrow, int m, int bins, int64_t n,
+                     float *d_ism)
 {
     if (m <= 0) return ISO_OK;
     const int64_t pairs = (int64_t)m * m;
     const int64_t ctas = (pairs + R32_PAIRS - 1) / R32_PAIRS;
     if (ctas > 0x7fffffff) return iso_fail(ISO_ERR_ARG, "reference FP32 MI: too many pairs");
-    const size_t smem = ((size_t)R32_PAIRS * (R32_TILE + 1) + (size_t)R32_PAIRS * bins) * sizeof(uint32_t);
+    void *tab;
+    ISO_TRY(iso_buf(ctx, BUF_LOGF_TABLE, (size_t)R32_LOG_TABLE * sizeof(float), &tab));
+    logf_table_kernel<<<R32_LOG_TABLE / 256, 256, 0, ctx->stream>>>((float *)tab);
+    ISO_LAUNCHED(ctx);
     // the reference converts its int field size to float (JointHistogram.cu:24, :159)
     const float nv = (float)n;
-    mi_ref32_kernel<<<(unsigned)ctas, R32_PAIRS, smem, ctx->stream>>>(d_joint, pairs, bins, nv, d_ism);
+    mi_ref32_kernel<<<(unsigned)ctas, R32_PAIRS, 0, ctx->stream>>>(d_joint, d_colrow, pairs, bins, nv,
+                                                                   (const float *)tab, d_ism);
     ISO_LAUNCHED(ctx);
     return ISO_OK;
 }

@@ -573,7 +573,8 @@ int iso_run_surfaces(iso_ctx *ctx, const float *d_vol, int X, int Y, int Z, cons
             need += 4.0 * m * ctx->plan_stride;  // the fields' precomputed row buckets
         }
         // the reference's FP32 MI keeps every ordered pair's histogram
-        if (ctx->mi_mode == ISO_MI_REF32) need += 4.0 * m * m * ctx->plan_bins * ctx->plan_bins;
+        if (ctx->mi_mode == ISO_MI_REF32)
+            need += 4.0 * m * m * ctx->plan_bins * ctx->plan_bins + 8.0 * m * m * ctx->plan_bins;
         need *= 1.15;  // arena growth slack
         if (ctx->admit(ctx->admit_user, (size_t)need) != 0)
             return iso_fail(ISO_ERR_NOMEM, "request needs %.0f bytes of device memory; over the budget", need);
