@@ -955,14 +955,35 @@ __global__ void __launch_bounds__(MI_THREADS) joint_mi_kernel(MiArgs a)
         static_assert((MI_THREADS * 4) % FB == 0, "one column group per thread");
         const uint4 *gh4 = reinterpret_cast<const uint4 *>(gh);
         uint4 cs4 = make_uint4(0u, 0u, 0u, 0u);
+        // the transposed dump (pair (j, i)) goes through a shared tile of
+        // T_ROWS rows (dynamic shared memory, present only when dumping), so
+        // that each of its rows leaves as whole 128-byte warp stores
+        constexpr int T_ROWS = 32, T_STRIDE = FB + 1;
+        extern __shared__ uint32_t s_tile[];  // [T_ROWS][T_STRIDE]
+        const bool transpose = dump && a.symmetric && i != j;
+        uint32_t *dump_ij = dump ? a.joint_dump + ((size_t)i * a.m + j) * FB * FB : nullptr;
+        uint32_t *dump_ji = transpose ? a.joint_dump + ((size_t)j * a.m + i) * FB * FB : nullptr;
         for (int q = threadIdx.x; q < FB * FB / 4; q += MI_THREADS) {
             const uint4 c = __ldcs(gh4 + q);
             const int r = q / (FB / 4), col = (q % (FB / 4)) * 4;
             if (dump) {
-                const uint32_t cv[4] = {c.x, c.y, c.z, c.w};
-                for (int e = 0; e < 4; ++e) {
-                    a.joint_dump[(((size_t)i * a.m + j) * FB + r) * FB + col + e] = cv[e];
-                    if (a.symmetric && i != j) a.joint_dump[(((size_t)j * a.m + i) * FB + col + e) * FB + r] = cv[e];
+                reinterpret_cast<uint4 *>(dump_ij)[q] = c;
+                if (transpose) {
+                    uint32_t *t = s_tile + (r % T_ROWS) * T_STRIDE + col;
+                    t[0] = c.x;
+                    t[1] = c.y;
+                    t[2] = c.z;
+                    t[3] = c.w;
+                    // every thread runs the same iterations: the block meets
+                    // here after each T_ROWS rows
+                    if ((q / MI_THREADS + 1) % (T_ROWS * FB / 4 / MI_THREADS) == 0) {
+                        __syncthreads();
+                        const int r0 = r - r % T_ROWS;
+                        const int w = threadIdx.x >> 5;
+                        for (int oc = w; oc < FB; oc += MI_THREADS / 32)
+                            dump_ji[(size_t)oc * FB + r0 + lane] = s_tile[lane * T_STRIDE + oc];
+                        __syncthreads();
+                    }
                 }
             }
             if (c.x) hxy -= clnc_of(a.clnc, c.x);
@@ -1330,7 +1351,9 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
             ma.ism = d_ism;
             ma.joint_dump = d_joint_dump;
             ma.colrow_dump = d_colrow_dump;
-            (bins == 256 ? joint_mi_kernel<256> : joint_mi_kernel<0>)<<<np, MI_THREADS, 0, ctx->stream>>>(ma);
+            // the 256-bin kernel's transposed dump tile: 32 rows of 257 words
+            const size_t mi_smem = (bins == 256 && d_joint_dump && symmetric) ? (size_t)32 * 257 * sizeof(uint32_t) : 0;
+            (bins == 256 ? joint_mi_kernel<256> : joint_mi_kernel<0>)<<<np, MI_THREADS, mi_smem, ctx->stream>>>(ma);
             ISO_LAUNCHED(ctx);
         }
         return ISO_OK;
