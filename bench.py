@@ -324,7 +324,8 @@ def run_ours(args):
     if rank == 0 and args.serving_requests > 0:
         ctx.close()
         ctx = None
-        batched, one, desc = serving_stats(args.serving_requests, args.rate, args.slots, args.budget_gb)
+        batched, one, desc = serving_stats(args.serving_requests, args.rate, args.slots, args.budget_gb,
+                                           mi=args.mi)
         line["serving"] = {"workload": desc, "continuous_batching": batched, "one_at_a_time": one}
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -615,7 +616,7 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def serving_stats(requests, rate, slots, budget_gb, max_wait_ms=2000.0):
+def serving_stats(requests, rate, slots, budget_gb, max_wait_ms=2000.0, mi="ref32"):
     """Poisson stream of ISM requests through the serving loop (continuous
     batching under an HBM budget) and through one-request-at-a-time serving.
     Shapes, isovalue counts and bins are drawn per request (seeded); volumes
@@ -657,6 +658,7 @@ def serving_stats(requests, rate, slots, budget_gb, max_wait_ms=2000.0):
     def serve(slots, policy):
         with isosim.Server(0, slots=slots, budget_bytes=int(budget_gb * (1 << 30))) as srv:
             srv.set_policy(policy, max_wait_ms)
+            srv.set_mi_mode(isosim.MI_REF32 if mi == "ref32" else isosim.MI_FP64)
             # warm each worker's arena on a small request
             for _ in range(slots):
                 srv.wait(srv.submit(pool[(shapes[0], "blobs")], shapes[0], reqs[0][3][:16], bins=128))
@@ -690,13 +692,14 @@ def serving_stats(requests, rate, slots, budget_gb, max_wait_ms=2000.0):
     batched = serve(slots, isosim.SERVE_SHORTEST_FIRST)
     plain = serve(1, isosim.SERVE_FIFO)
     desc = ("Poisson stream of %d requests at %g req/s; shapes %s; isovalues {16..256}; bins {128,256}; "
-            "%g GB HBM budget; %d slots; small requests: work estimate at or below the median"
-            % (requests, rate, shapes, budget_gb, slots))
+            "%g GB HBM budget; %d slots; %s MI; small requests: work estimate at or below the median"
+            % (requests, rate, shapes, budget_gb, slots,
+               "the reference's FP32" if mi == "ref32" else "FP64"))
     return batched, plain, desc
 
 
 def run_serving(args):
-    batched, plain, desc = serving_stats(args.requests, args.rate, args.slots, args.budget_gb)
+    batched, plain, desc = serving_stats(args.requests, args.rate, args.slots, args.budget_gb, mi=args.mi)
     line = {"metric": "ISM pairs/sec and p50/p99 latency, serving", "value": batched["pairs_per_s"],
             "unit": "pairs/s", "n_gpus": 1, "higher_is_better": True, "data": "synthetic (seeded)",
             "config": {"workload": desc, "slots": args.slots},

@@ -388,6 +388,10 @@ ISO_API int iso_server_create(int device, int slots, size_t hbm_budget_bytes, is
 #define ISO_SERVE_FIFO 0
 #define ISO_SERVE_SHORTEST_FIRST 1
 ISO_API int iso_server_set_policy(iso_server *s, int policy, double max_wait_ms);
+/* Applies iso_ctx_set_limit(which, value) to every worker context (for
+ * example ISO_LIMIT_MI_MODE for the reference's own FP32 MI).  Only while no
+ * request is queued or running; ISO_ERR_ARG otherwise. */
+ISO_API int iso_server_set_limit(iso_server *s, int which, int64_t value);
 /* Queues a request (the descriptor is copied; the buffers must stay valid
  * until iso_server_wait returns for its ticket). */
 ISO_API int iso_server_submit(iso_server *s, const iso_request *req, int64_t *ticket);

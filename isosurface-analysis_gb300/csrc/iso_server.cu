@@ -270,6 +270,23 @@ extern "C" int iso_server_set_policy(iso_server *s, int policy, double max_wait_
     return ISO_OK;
 }
 
+extern "C" int iso_server_set_limit(iso_server *s, int which, int64_t value)
+{
+    iso_clear_error();
+    if (!s) return iso_fail(ISO_ERR_ARG, "iso_server_set_limit: bad argument");
+    std::lock_guard<std::mutex> lock(s->mu);
+    // a worker reads its context's settings while it runs a request: only an
+    // idle server takes new ones
+    bool busy = !s->queue.empty();
+    for (const Worker &k : s->workers) busy = busy || k.state != WState::Idle;
+    if (busy) return iso_fail(ISO_ERR_ARG, "iso_server_set_limit: requests are queued or running");
+    for (Worker &k : s->workers) {
+        const int rc = iso_ctx_set_limit(k.ctx, which, value);
+        if (rc != ISO_OK) return rc;
+    }
+    return ISO_OK;
+}
+
 extern "C" int iso_server_submit(iso_server *s, const iso_request *req, int64_t *ticket)
 {
     iso_clear_error();

@@ -120,6 +120,7 @@ def _load():
         "iso_server_get_stats": (C.c_int, [P, C.POINTER(ServerStats)]),
         "iso_server_destroy": (None, [P]),
         "iso_server_set_policy": (C.c_int, [P, C.c_int, C.c_double]),
+        "iso_server_set_limit": (C.c_int, [P, C.c_int, C.c_int64]),
         "iso_similarity_map_noalloc": (C.c_int, [P, C.c_int, C.c_int64, C.c_int64, C.c_int, P, P]),
         "iso_pair_map": (C.c_int, [P, P, C.c_int, C.c_int64, C.c_int64, C.c_int, P, C.c_int64, P]),
         "iso_probe_counter_rate": (C.c_int, [P, C.c_int, C.POINTER(C.c_double)]),
@@ -406,6 +407,14 @@ class Server:
         """SERVE_FIFO or SERVE_SHORTEST_FIRST (smallest work estimate first,
         the oldest request first once it waited max_wait_ms)."""
         _check(lib.iso_server_set_policy(self.handle, int(policy), float(max_wait_ms)))
+
+    def set_limit(self, which, value):
+        """iso_ctx_set_limit on every worker context (only while idle)."""
+        _check(lib.iso_server_set_limit(self.handle, int(which), int(value)))
+
+    def set_mi_mode(self, mode):
+        """MI_FP64 or MI_REF32 for every request (only while idle)."""
+        self.set_limit(4, mode)
 
     def stats(self):
         st = ServerStats()

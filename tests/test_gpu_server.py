@@ -122,3 +122,23 @@ def test_shortest_first_policy():
         for k, t in enumerate(tickets):
             ism, ids, _ = srv.wait(t)
             assert np.array_equal(ism, alone[k % len(reqs)][0])
+
+
+def test_reference_mi_mode_through_the_server():
+    """The server's workers in the reference's FP32 MI mode: every request's
+    map equals a context's map in that mode bit for bit; the setting is
+    refused while requests are queued or running."""
+    import isosim
+    reqs = requests()
+    with isosim.Context(0) as ctx:
+        ctx.set_mi_mode(isosim.MI_REF32)
+        alone = [ctx.ism(v, d, i, surface=s, bins=b)[:2] for v, d, i, s, b in reqs]
+    with isosim.Server(0, slots=2, budget_bytes=4 << 30) as srv:
+        srv.set_mi_mode(isosim.MI_REF32)
+        tickets = [srv.submit(v, d, i, surface=s, bins=b) for v, d, i, s, b in reqs]
+        with pytest.raises(isosim.IsoError):
+            srv.set_mi_mode(isosim.MI_FP64)   # requests are queued or running
+        for k, t in enumerate(tickets):
+            ism, ids, _ = srv.wait(t)
+            assert np.array_equal(ids, alone[k][1]) and np.array_equal(ism, alone[k][0]), k
+        srv.set_mi_mode(isosim.MI_FP64)       # idle again
