@@ -15,15 +15,16 @@ libcuda.so.1) and drives its kernel calculate_histogram_g (JointHistogram.cu:
   * fields staged in chunks of MAX_PER_RUN = 1,000,000 values at stride
     MAX_PER_RUN (:383-394), one kernel launch per chunk, the last chunk
     flagged so the kernel evaluates calculateMutualInformation (:156-160);
-  * the run-info values of calculateRunInfo (:231-264) for the case where all
-    m*m histograms fit one allocation of MALLOC_MAX_BYTES (2 GiB,
-    isosurfaces_cuda/hdr/common.h:8).
+  * the runs of calculateRunInfo (:231-264): as many as the m*m histograms
+    need at MALLOC_MAX_BYTES (2 GiB, isosurfaces_cuda/hdr/common.h:8) per
+    allocation, each over every field chunk.
 
 The result is the reference's own output on the GPU: its FP32 similarity map
 (every ordered pair), its joint histograms, and its column and row sums.
-Sizes that need several histogram runs, or whose last chunk would be empty
-(the reference's loop skips a chunk when the field length is a multiple of
-MAX_PER_RUN), are refused here rather than run.
+Sizes whose last chunk would be empty (the reference's loop skips a chunk
+when the field length is a multiple of MAX_PER_RUN), and sizes where the
+kernel's 32-bit histogram index overflows onto other pairs' histograms, are
+refused here rather than run.
 """
 import ctypes as C
 import os
@@ -149,14 +150,41 @@ def _account(timing, name, ms):
         timing[name] = timing.get(name, 0.0) + ms
 
 
+def run_info(num_tasks, hist_bytes, num_hist):
+    """calculateRunInfo (JointHistogram.cu:231-264), integer for integer:
+    (tasksPerRun, lastRunMemBytes, histMemMax, offsetMax, memoryPerRun, odd).
+    offsetMax runs of tasksPerRun tasks share one allocation of memoryPerRun
+    bytes; with an odd task count over several runs, one more run takes the
+    last task alone."""
+    offset_max, hist_mem_max = 1, hist_bytes
+    if hist_bytes > MALLOC_MAX_BYTES:
+        offset_max = 2
+        while offset_max * MALLOC_MAX_BYTES < hist_bytes:
+            offset_max += 1
+        hist_mem_max = hist_bytes // offset_max
+    last_run = hist_mem_max
+    tasks_per_run = num_tasks // offset_max
+    odd = num_tasks % 2 == 1 and offset_max > 1
+    mem_per_run = hist_mem_max
+    mem_per_hist = hist_bytes // num_hist
+    if odd:
+        mem_per_run = hist_mem_max - mem_per_hist // offset_max
+        offset_max += 1
+        last_run = mem_per_hist
+    return tasks_per_run, last_run, hist_mem_max, offset_max, mem_per_run, odd
+
+
 def similarity(fields, bins, mins=None, maxs=None, multi=False, block=128, timing=None):
     """The reference's calculate_histogram_h on the GPU for m fields (2m rows
     in multi mode: the first m against the last m).  fields: [rows, F]
     float32.  mins/maxs: per-row interval (default: each row's min and max,
     the values DistanceField::getInterval gives for non-negative fields).
-    Returns (sim [m, m] float32, joint [m*m, bins, bins] uint32,
-    col_sums [m*m, bins], row_sums [m*m, bins]).  timing (a dict), if given,
-    accumulates the device ms of each kernel by name."""
+    Runs as many histogram runs as calculateRunInfo gives, each over every
+    1,000,000-value chunk of the fields (JointHistogram.cu:365-395).
+    Returns (sim [m, m] float32, joint [m*m, bins, bins] uint32 or None when
+    the map takes several runs (the reference keeps only one run's histograms
+    at a time), col_sums [m*m, bins], row_sums [m*m, bins]).  timing (a
+    dict), if given, accumulates the device ms of each kernel by name."""
     drv = _driver()
     fields = np.ascontiguousarray(fields, dtype=np.float32)
     rows, F = fields.shape
@@ -166,16 +194,22 @@ def similarity(fields, bins, mins=None, maxs=None, multi=False, block=128, timin
         maxs = fields.max(axis=1)
     mins = np.ascontiguousarray(mins, np.float32)
     maxs = np.ascontiguousarray(maxs, np.float32)
-    hist_bytes = m * m * bins * bins * 4
-    if hist_bytes > MALLOC_MAX_BYTES:
-        raise ValueError("more than one histogram run: not driven by this harness")
     if F % MAX_PER_RUN == 0:
         raise ValueError("field length a multiple of MAX_PER_RUN: the reference skips its last chunk")
     num_tasks = m * m
+    hist_bytes = num_tasks * bins * bins * 4
+    max_size = run_info(num_tasks, hist_bytes, num_tasks)[4] // 4
+    if num_tasks * bins * bins > 2 ** 31 and max_size & (max_size - 1):
+        # the kernel's histogram index (id1 * m + id2) * bins^2 + bin is a
+        # 32-bit int (JointHistogram.cu:133-135, :151); once it wraps, its
+        # value modulo a run size that is not a power of two lands in other
+        # pairs' histograms
+        raise ValueError("the reference's 32-bit histogram index wraps onto other pairs' histograms here")
     if multi:
         tasks = np.array([(i, j + m) for i in range(m) for j in range(m)], np.int32)
     else:
         tasks = np.array([(i, j) for i in range(m) for j in range(m)], np.int32)
+    tasks_per_run, last_run, hist_mem_max, offset_max, mem_per_run, odd = run_info(num_tasks, hist_bytes, num_tasks)
     bufs = []
 
     def alloc(nbytes):
@@ -191,46 +225,50 @@ def similarity(fields, bins, mins=None, maxs=None, multi=False, block=128, timin
         d_row = alloc(m * m * bins * 4)
         d_sim = alloc(m * m * 4)
         d_tasks = alloc(num_tasks * 8)
-        d_joint = alloc(hist_bytes)
+        d_joint = alloc(mem_per_run)
         drv.memset0(d_col, m * m * bins * 4)
         drv.memset0(d_row, m * m * bins * 4)
         drv.memset0(d_sim, m * m * 4)
-        drv.memset0(d_joint, hist_bytes)
         drv.h2d(d_min, mins)
         drv.h2d(d_max, maxs)
         drv.h2d(d_tasks, tasks)
-        # calculateRunInfo with one run: every ordered pair in it, histograms
-        # indexed modulo their total size
-        ri = RunInfo(tasksPerRun=num_tasks, lastRunMemBytes=hist_bytes, histMemMax=hist_bytes, offsetMax=1,
-                     memoryPerRun=hist_bytes, odd=False, maxSize=hist_bytes // 4, fieldMaxMemory=0,
-                     fieldsLastRun=False, fieldsLastRunBytes=0, multi=multi)
+        ri = RunInfo(tasksPerRun=tasks_per_run, lastRunMemBytes=last_run, histMemMax=hist_mem_max,
+                     offsetMax=offset_max, memoryPerRun=mem_per_run, odd=odd, maxSize=mem_per_run // 4,
+                     fieldMaxMemory=0, fieldsLastRun=False, fieldsLastRunBytes=0, multi=multi)
         di = DataInfo(F, bins, m, m)
-        grid = (num_tasks + block - 1) // block
-        for off in range(0, F, MAX_PER_RUN):
-            count = MAX_PER_RUN
-            if off + MAX_PER_RUN >= F:
-                ri.fieldsLastRun = True
-                ri.fieldsLastRunBytes = F % MAX_PER_RUN
-                count = ri.fieldsLastRunBytes
-            chunk = np.zeros((rows, MAX_PER_RUN), np.float32)
-            chunk[:, :count] = fields[:, off:off + count]
-            drv.h2d(d_fields, chunk)
-            args = [C.c_uint64(d_fields), C.c_uint64(d_min), C.c_uint64(d_max), C.c_uint64(d_joint),
-                    C.c_uint64(d_col), C.c_uint64(d_row), C.c_uint64(d_tasks), C.c_ulong(0), C.c_ulong(off),
-                    C.c_uint64(d_sim), ri, di]
-            _account(timing, "calculate_histogram_g", drv.launch(grid, block, args))
+        grid = (tasks_per_run + block - 1) // block
+        chunk = np.zeros((rows, MAX_PER_RUN), np.float32)
+        for run in range(offset_max):
+            drv.memset0(d_joint, mem_per_run)
+            ri.fieldsLastRun = False
+            for off in range(0, F, MAX_PER_RUN):
+                count = MAX_PER_RUN
+                if off + MAX_PER_RUN >= F:
+                    ri.fieldsLastRun = True
+                    ri.fieldsLastRunBytes = F % MAX_PER_RUN
+                    count = ri.fieldsLastRunBytes
+                chunk[:] = 0
+                chunk[:, :count] = fields[:, off:off + count]
+                drv.h2d(d_fields, chunk)
+                args = [C.c_uint64(d_fields), C.c_uint64(d_min), C.c_uint64(d_max), C.c_uint64(d_joint),
+                        C.c_uint64(d_col), C.c_uint64(d_row), C.c_uint64(d_tasks), C.c_ulong(run), C.c_ulong(off),
+                        C.c_uint64(d_sim), ri, di]
+                _account(timing, "calculate_histogram_g", drv.launch(grid, block, args))
         sim = np.zeros(m * m, np.float32)
-        joint = np.zeros(m * m * bins * bins, np.uint32)
         col = np.zeros(m * m * bins, np.uint32)
         row = np.zeros(m * m * bins, np.uint32)
         drv.d2h(sim, d_sim)
-        drv.d2h(joint, d_joint)
         drv.d2h(col, d_col)
         drv.d2h(row, d_row)
+        joint = None
+        if offset_max == 1:
+            joint = np.zeros(m * m * bins * bins, np.uint32)
+            drv.d2h(joint, d_joint)
+            joint = joint.reshape(m * m, bins, bins)
     finally:
         for p in bufs:
             drv.free(p)
-    return sim.reshape(m, m), joint.reshape(m * m, bins, bins), col.reshape(m * m, bins), row.reshape(m * m, bins)
+    return sim.reshape(m, m), joint, col.reshape(m * m, bins), row.reshape(m * m, bins)
 
 
 # ---------------------------------------------------------------------------

@@ -122,3 +122,26 @@ def test_multi_mode_cross_map():
         c.set_mi_mode(isosim.MI_REF32)
         cm = c.cross_map(a, b, bins=256)
     assert np.array_equal(cm, sim)
+
+
+@pytest.mark.parametrize("m", [96, 91])
+def test_several_histogram_runs(m):
+    """Maps whose histograms exceed one 2 GiB allocation at 256 bins, as the
+    256^3 workload's do: 96 fields take two runs of 4,608 pairs, 91 fields
+    (an odd pair count) two runs of 4,140 and a last run of one pair
+    (calculateRunInfo, JointHistogram.cu:231-264); fields of 1,200,001 values
+    in two chunks.  The reference-named entry's map and sums against the
+    reference kernel's, bit for bit."""
+    import isosim
+    assert refgpu.run_info(m * m, m * m * 65536 * 4, m * m)[3] == (2 if m == 96 else 3)
+    rng = np.random.default_rng(m)
+    n = 1200001
+    base = rng.uniform(0, 1, n)
+    f = np.stack([np.abs(base * (1 + 0.02 * k) + 0.1 * rng.standard_normal(n)) for k in range(m)]).astype(np.float32)
+    sim, joint, cols, rows = refgpu.similarity(f, 256)
+    assert joint is None
+    mins, maxs = f.min(axis=1), f.max(axis=1)
+    hsim, hcols, hrows = isosim.calculate_histogram_h(list(f), mins, maxs, 256)
+    assert np.array_equal(hcols.reshape(m * m, 256), cols)
+    assert np.array_equal(hrows.reshape(m * m, 256), rows)
+    assert np.array_equal(hsim, sim)
