@@ -145,3 +145,30 @@ def test_several_histogram_runs(m):
     assert np.array_equal(hcols.reshape(m * m, 256), cols)
     assert np.array_equal(hrows.reshape(m * m, 256), rows)
     assert np.array_equal(hsim, sim)
+
+
+def test_config3_full_length_fields():
+    """The 256^3 benchmark workload's own distance fields at full length
+    (16,777,216 values: 16 chunks of 1,000,000 and a last one of 777,216),
+    every fourth of its 256 fields (4,096 ordered pairs, one histogram run;
+    the runs themselves are pinned above): the reference-named entry's map and
+    sums against the reference kernel's, bit for bit, and the pipeline's
+    ISO_MI_REF32 map on the same pairs."""
+    import isosim
+    import isosim.synth as synth
+    vol, isos, bins = synth.config3()
+    F = 256 ** 3
+    with isosim.Context(0) as c:
+        c.set_mi_mode(isosim.MI_REF32)
+        ism32, ids, _, _ = c.ism(vol.ravel(), (256, 256, 256), isos, bins=bins)
+        rows = list(range(0, len(ids), 4))
+        fields = np.stack([c.copy_field(r, np.zeros(F, np.float32)) for r in rows])
+    m = len(rows)
+    sim, joint, cols, rws = refgpu.similarity(fields, bins)
+    assert joint is not None and m == 64
+    mins, maxs = fields.min(axis=1), fields.max(axis=1)
+    hsim, hcols, hrows = isosim.calculate_histogram_h(list(fields), mins, maxs, bins)
+    assert np.array_equal(hcols.reshape(m * m, bins), cols)
+    assert np.array_equal(hrows.reshape(m * m, bins), rws)
+    assert np.array_equal(hsim, sim)
+    assert np.array_equal(ism32[np.ix_(rows, rows)], sim)
