@@ -16,6 +16,8 @@
 #   ref_bvh.cubin        device code of BVH.cu (the reference's own LBVH build
 #                        and traversal) with oracle/ref_bvh_wrap.cu, nvcc
 #                        defaults
+#   ref_approx.cubin     device code of IsosurfaceApproximation.cu (the
+#                        reference's voxel-approximation kernel), nvcc defaults
 # Runs only where the reference tree exists.
 # Usage: oracle/build_ref.sh [reference_root]   (default: $ISO_REFERENCE_ROOT,
 #        else /root/reference)
@@ -41,9 +43,11 @@ nvcc -std=c++17 -cubin "${ARCH[@]}" -w -include "$HERE/refshim_mc/refshim_textur
   "$HERE/ref_mc_wrap.cu" -o "$OUT/ref_mc.cubin" &
 nvcc -std=c++17 -cubin "${ARCH[@]}" -w -I"$HERE/refshim" -I"$LIB" \
   "$HERE/ref_bvh_wrap.cu" -o "$OUT/ref_bvh.cubin" &
+nvcc -std=c++17 -cubin "${ARCH[@]}" -w -I"$HERE/refshim" -I"$LIB" \
+  "$LIB/isosurfaces_cuda/src/IsosurfaceApproximation.cu" -o "$OUT/ref_approx.cubin" &
 wait
 nvcc -shared -Xcompiler -fPIC "$OUT/ref_histogram_wrap.o" "$OUT/ref_approx_wrap.o" "$OUT/common.o" -o "$OUT/libisoref.so"
 # where the sources were found, for the CPU tests that read the reference's
 # tables directly (oracle.reference_root())
 echo "$REF" > "$OUT/reference_root.txt"
-echo "built $OUT/libisoref.so and the reference cubins (histogram, marching cubes, LBVH)"
+echo "built $OUT/libisoref.so and the reference cubins (histogram, marching cubes, LBVH, approximation)"

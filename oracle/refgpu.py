@@ -1,6 +1,8 @@
-"""The reference's own GPU kernels -- its joint histogram and its marching
-cubes -- run on this machine's GPU (test infrastructure only: a checker,
-never the engine).  The marching-cubes harness is marching_cubes() below.
+"""The reference's own GPU kernels -- its joint histogram, marching cubes,
+LBVH and voxel approximation -- run on this machine's GPU (test
+infrastructure only: a checker, never the engine).  The histogram harness is
+similarity(); marching_cubes(), lbvh_distance_field() and approximation()
+follow below.
 
 oracle/build_ref.sh compiles isosurfaces_cuda/src/JointHistogram.cu from the
 reference's sources, device code only and with nvcc's default flags (as the
@@ -106,8 +108,8 @@ class _Driver:
     def d2h(self, arr, src):
         self._check(self.cu.cuMemcpyDtoH_v2(arr.ctypes.data, src, arr.nbytes), "cuMemcpyDtoH")
 
-    def memset0(self, p, nbytes):
-        self._check(self.cu.cuMemsetD8_v2(p, 0, nbytes), "cuMemsetD8")
+    def memset0(self, p, nbytes, value=0):
+        self._check(self.cu.cuMemsetD8_v2(p, value, nbytes), "cuMemsetD8")
 
     def function(self, cubin, name):
         """A kernel of a cubin under oracle/_ref/ (each cubin loaded once)."""
@@ -540,3 +542,56 @@ def lbvh_distance_field(points, dims, ds=1, num_samples=BVH_NUM_SAMPLES, timing=
         for p in bufs:
             drv.free(p)
     return out
+
+
+
+# ---------------------------------------------------------------------------
+# Voxel approximation: the reference's calculate_approximation_g
+# (isosurfaces_cuda/src/IsosurfaceApproximation.cu:120-135), compiled from its
+# sources by oracle/build_ref.sh into oracle/_ref/ref_approx.cubin.
+APPROX_CUBIN = os.path.join(HERE, "_ref", "ref_approx.cubin")
+APPROX_KERNEL = b"_Z25calculate_approximation_gPffiiiP4int3iii"
+APPROX_THREADS = 256              # IsosurfaceApproximation.cu:162
+APPROX_MAX_BLOCKS = 2 << 14       # :163
+
+
+def approx_available():
+    return os.path.exists(APPROX_CUBIN)
+
+
+def approximation(volume, dims, iso, timing=None):
+    """The reference's approximate_isosurfaces_h (IsosurfaceApproximation.cu:
+    159-208) at scale 1 with its own kernel on this GPU: the cell array set to
+    all-ones bytes, launches of 32,768 blocks of 256 threads at block offsets
+    0, 32768, ... until the volume is covered, then the stable compaction of
+    the cells whose x is not negative (thrust::copy_if with is_positive,
+    thrustWrapper.h:47-54; here on the host).  volume: X*Y*Z float32 with z
+    fastest.  Returns the crossing cells as int32 [k, 3] in linear order."""
+    drv = _driver()
+    X, Y, Z = (int(d) for d in dims)
+    V = X * Y * Z
+    vol = np.ascontiguousarray(volume, np.float32).ravel()
+    if vol.size != V or min(X, Y, Z) < 2:
+        raise ValueError("volume size does not match dims, or a dimension below 2")
+    num_cells = (X - 1) * (Y - 1) * (Z - 1)
+    fn = drv.function(APPROX_CUBIN, APPROX_KERNEL)
+    bufs = []
+    try:
+        d_vol = drv.alloc(V * 4)
+        bufs.append(d_vol)
+        d_cells = drv.alloc(num_cells * 12)
+        bufs.append(d_cells)
+        drv.h2d(d_vol, vol)
+        drv.memset0(d_cells, num_cells * 12, 0xFF)
+        blocks = (V + APPROX_THREADS - 1) // APPROX_THREADS
+        for off in range(0, blocks, APPROX_MAX_BLOCKS):
+            _account(timing, "calculate_approximation_g", drv.launch(
+                APPROX_MAX_BLOCKS, APPROX_THREADS,
+                [C.c_uint64(d_vol), C.c_float(iso), C.c_int(X), C.c_int(Y), C.c_int(Z), C.c_uint64(d_cells),
+                 C.c_int(V), C.c_int(off), C.c_int(1)], fn))
+        cells = np.zeros((num_cells, 3), np.int32)
+        drv.d2h(cells, d_cells)
+    finally:
+        for p in bufs:
+            drv.free(p)
+    return np.ascontiguousarray(cells[cells[:, 0] >= 0])
