@@ -10,19 +10,20 @@ reference's CMake build passes none), into oracle/_ref/ref_histogram.cubin.
 This module loads that cubin through the CUDA driver API (ctypes on
 libcuda.so.1) and drives its kernel calculate_histogram_g (JointHistogram.cu:
 100-162) the way the reference's host function calculate_histogram_h
-(JointHistogram.cu:266-420) does for a single histogram run:
+(JointHistogram.cu:266-420) does:
 
   * one task per ordered pair, (i, j) for i, j < m in row-major order, or
     (i, j + m) in multi mode (:306-328);
   * fields staged in chunks of MAX_PER_RUN = 1,000,000 values at stride
-    MAX_PER_RUN (:383-394), one kernel launch per chunk, the last chunk
+    MAX_PER_RUN (:377-392), one kernel launch per chunk, the last chunk
     flagged so the kernel evaluates calculateMutualInformation (:156-160);
   * the runs of calculateRunInfo (:231-264): as many as the m*m histograms
     need at MALLOC_MAX_BYTES (2 GiB, isosurfaces_cuda/hdr/common.h:8) per
     allocation, each over every field chunk.
 
 The result is the reference's own output on the GPU: its FP32 similarity map
-(every ordered pair), its joint histograms, and its column and row sums.
+(every ordered pair), its column and row sums, and its joint histograms when
+the map takes one run.
 Sizes whose last chunk would be empty (the reference's loop skips a chunk
 when the field length is a multiple of MAX_PER_RUN), and sizes where the
 kernel's 32-bit histogram index overflows onto other pairs' histograms, are
@@ -182,7 +183,7 @@ def similarity(fields, bins, mins=None, maxs=None, multi=False, block=128, timin
     float32.  mins/maxs: per-row interval (default: each row's min and max,
     the values DistanceField::getInterval gives for non-negative fields).
     Runs as many histogram runs as calculateRunInfo gives, each over every
-    1,000,000-value chunk of the fields (JointHistogram.cu:365-395).
+    1,000,000-value chunk of the fields (JointHistogram.cu:372-392).
     Returns (sim [m, m] float32, joint [m*m, bins, bins] uint32 or None when
     the map takes several runs (the reference keeps only one run's histograms
     at a time), col_sums [m*m, bins], row_sums [m*m, bins]).  timing (a
