@@ -292,6 +292,14 @@ ISO_API int iso_copy_joint_histogram(iso_ctx *ctx, int i, int j, uint32_t *out);
  * histogram stage.  bins: a power of two in [2, 256]. */
 ISO_API int iso_probe_counter_rate(iso_ctx *ctx, int bins, double *updates_per_s);
 
+/* Failure-detection probe: runs the bounded barrier wait that the
+ * tensor-core distance kernel uses (a wait that gives up after a time limit,
+ * after which the kernel reports an error and returns) on a barrier that one
+ * thread arrives at first (arrive != 0) or that nothing arrives at (arrive =
+ * 0).  *timed_out is 1 when the wait gave up after limit_ns nanoseconds (at
+ * most 1e10), 0 when it completed; the context stays usable either way. */
+ISO_API int iso_probe_wait_timeout(iso_ctx *ctx, int arrive, int64_t limit_ns, int *timed_out);
+
 /* ---------------------------------------------------------------------- */
 /* Reference-named entry points (drop-in for isosurfaces_cuda/funcs.h)     */
 /* ---------------------------------------------------------------------- */

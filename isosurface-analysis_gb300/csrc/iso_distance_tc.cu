@@ -29,6 +29,11 @@
 //    the smallest value B of its columns and recomputes the canonical FP32
 //    distance of every point within tau of B; the two halves' minima are
 //    merged at the end.
+//  * Every barrier wait gives up after 2 s of the global timer.  A CTA whose
+//    wait gave up waits (with the same limit) for its copies still in flight
+//    and its last MMA, frees its tensor memory and raises the launch's error
+//    flag, which the host returns as ISO_ERR_INTERNAL; iso_probe_wait_timeout
+//    exercises the same wait on a barrier that nothing arrives at.
 //
 // Exactness: the canonical winner w (smallest canonical FP32 distance) is
 // always a candidate: with e the error of A.B against the exact
@@ -72,7 +77,7 @@ constexpr int SM_BAR = SM_BEST + 128 * 4;  // loaded[STAGES], consumed[STAGES], 
 constexpr int SM_USED = SM_BAR + (2 * STAGES + 2) * 8 + 16;
 constexpr int SM_ALLOC = 80 * 1024;
 constexpr float SENTINEL_Q = 30000.0f;        // |p|^2 of padding rows: never within tau
-constexpr uint32_t WAIT_LIMIT = 1u << 26;     // polls of one barrier wait before giving up
+constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // one barrier wait gives up after 2 s
 
 __device__ __forceinline__ void split_f16(float v, __half &hi, __half &lo)
 {
@@ -240,7 +245,9 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
             const uint32_t idesc = tc_idesc_f16_f32(128, TC_POINTS);
             // sweep position i holds block (start + i) mod nb, in stage
             // i mod STAGES (phase (i / STAGES) & 1) and accumulator i & 1
+            int fetched = 0, landed = 0, issued = 0;  // positions copied, waited for, contracted
             auto fetch = [&](int i, int st) {
+                ++fetched;
                 int blk = start + i;
                 if (blk >= nb) blk -= nb;
                 const int64_t rest = P - (int64_t)blk * TC_POINTS;
@@ -254,14 +261,15 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
             int st = 0;
             uint32_t ph = 0;
             for (int i = 0; i < nb && ok; ++i) {
-                ok = mbar_wait(&loaded[st], ph, WAIT_LIMIT);
+                ok = mbar_wait(&loaded[st], ph, WAIT_LIMIT_NS);
                 if (!ok) break;
+                ++landed;
                 if (i >= 2) {
                     // position i - 2 read back: its accumulator (i % 2) and
                     // its stage are free; the stage takes position
                     // i - 2 + STAGES
                     const int sd = st >= 2 ? st - 2 : st + STAGES - 2;
-                    ok = mbar_wait(&consumed[sd], st >= 2 ? ph : ph ^ 1u, WAIT_LIMIT);
+                    ok = mbar_wait(&consumed[sd], st >= 2 ? ph : ph ^ 1u, WAIT_LIMIT_NS);
                     if (!ok) break;
                     if (i - 2 + STAGES < nb) fetch(i - 2 + STAGES, sd);
                 }
@@ -269,10 +277,18 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
                 tc_mma_f16(tbase + (uint32_t)(i & 1) * TC_POINTS, adesc, tc_desc(sm + SM_B0 + st * BLOCK_BYTES), idesc,
                            0);
                 tc_commit(&full[i & 1]);
+                ++issued;
                 if (++st == STAGES) {
                     st = 0;
                     ph ^= 1u;
                 }
+            }
+            if (!ok) {
+                // before the CTA gives its shared and tensor memory back: the
+                // copies still in flight and the last MMA, each with a limit
+                for (int q = landed; q < fetched; ++q)
+                    mbar_wait(&loaded[q % STAGES], (uint32_t)((q / STAGES) & 1), WAIT_LIMIT_NS);
+                if (issued > 0) mbar_wait(&full[(issued - 1) & 1], (uint32_t)(((issued - 1) >> 1) & 1), WAIT_LIMIT_NS);
             }
         }
         ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
@@ -284,7 +300,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
         int st = 0, blk = start;
         for (int i = 0; i < nb; ++i) {
             const int acc = i & 1;
-            ok = __all_sync(0xffffffffu, mbar_wait(&full[acc], (uint32_t)((i >> 1) & 1), WAIT_LIMIT));
+            ok = __all_sync(0xffffffffu, mbar_wait(&full[acc], (uint32_t)((i >> 1) & 1), WAIT_LIMIT_NS));
             if (!ok) break;
             tc_fence_after();
             uint32_t r[HALF];
@@ -331,7 +347,41 @@ __global__ void __launch_bounds__(TC_THREADS, 2) df_tc_kernel(TcArgs a)
     if (w == 0) tmem_dealloc(tbase, TC_COLS);
 }
 
+// Failure-detection probe: the kernels' bounded barrier wait on a barrier
+// that one thread arrives at first (arrive != 0) or that nothing arrives at;
+// the wait gives up after limit_ns and the kernel returns normally.
+__global__ void wait_probe_kernel(int arrive, uint64_t limit_ns, int *timed_out)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    if (arrive && threadIdx.x == 0) mbar_arrive(&bar);
+    __syncthreads();
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(&bar, 0, limit_ns));
+    if (threadIdx.x == 0) *timed_out = ok ? 0 : 1;
+}
+
 }  // namespace
+
+extern "C" int iso_probe_wait_timeout(iso_ctx *ctx, int arrive, int64_t limit_ns, int *timed_out)
+{
+    iso_clear_error();
+    if (!ctx || !timed_out || limit_ns < 0 || limit_ns > 10000000000ll)
+        return iso_fail(ISO_ERR_ARG, "iso_probe_wait_timeout: limit_ns must be in [0, 1e10]");
+    ISO_CUDA(cudaSetDevice(ctx->device));
+    void *d;
+    ISO_TRY(iso_buf(ctx, BUF_MISC, 256, &d));
+    int *flag = (int *)d;
+    ISO_CUDA(cudaMemsetAsync(flag, 0xff, sizeof(int), ctx->stream));
+    wait_probe_kernel<<<1, 32, 0, ctx->stream>>>(arrive, (uint64_t)limit_ns, flag);
+    ISO_LAUNCHED(ctx);
+    int h = -1;
+    ISO_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    ISO_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (h != 0 && h != 1) return iso_fail(ISO_ERR_INTERNAL, "iso_probe_wait_timeout: the probe did not report");
+    *timed_out = h;
+    return ISO_OK;
+}
 
 int iso_run_distance_tc(iso_ctx *ctx, const IsoSampleGrid &g, const IsoSegments &sg, const int64_t *h_seg_count, int m,
                         float *fields, int64_t stride)

@@ -89,12 +89,21 @@ __device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-// Waits for the phase with the given parity to complete, for at most `limit`
-// polls; returns false if it gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint32_t limit)
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits for the phase with the given parity to complete, for at most
+// limit_ns nanoseconds of the global timer (checked every 32 polls); returns
+// false if it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint64_t limit_ns)
 {
     const uint32_t a = smem_addr(mbar);
-    for (uint32_t i = 0; i < limit; ++i) {
+    const uint64_t t0 = global_ns();
+    for (uint32_t i = 0;; ++i) {
         uint32_t ok;
         asm volatile(
             "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
@@ -102,8 +111,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint3
             : "r"(a), "r"(parity)
             : "memory");
         if (ok) return true;
+        if ((i & 31u) == 31u && global_ns() - t0 > limit_ns) return false;
     }
-    return false;
 }
 
 // Arrival that also announces `bytes` of asynchronous copies the phase waits for.

@@ -124,6 +124,7 @@ def _load():
         "iso_similarity_map_noalloc": (C.c_int, [P, C.c_int, C.c_int64, C.c_int64, C.c_int, P, P]),
         "iso_pair_map": (C.c_int, [P, P, C.c_int, C.c_int64, C.c_int64, C.c_int, P, C.c_int64, P]),
         "iso_probe_counter_rate": (C.c_int, [P, C.c_int, C.POINTER(C.c_double)]),
+        "iso_probe_wait_timeout": (C.c_int, [P, C.c_int, C.c_int64, C.POINTER(C.c_int)]),
         "iso_block_similarity": (C.c_int, [P, P, C.c_int64, C.c_int, P, C.c_int64, P]),
     }
     for name, (res, args) in sig.items():
@@ -284,6 +285,14 @@ class Context:
         r = C.c_double()
         _check(lib.iso_probe_counter_rate(self.handle, bins, C.byref(r)))
         return r.value
+
+    def probe_wait_timeout(self, arrive, limit_ns):
+        """Runs the kernels' bounded barrier wait on a barrier that one thread
+        arrives at first (arrive) or that nothing arrives at; True when the
+        wait gave up after limit_ns."""
+        r = C.c_int()
+        _check(lib.iso_probe_wait_timeout(self.handle, 1 if arrive else 0, int(limit_ns), C.byref(r)))
+        return r.value == 1
 
     def copy_field(self, row, out):
         """Row `row` of the last ism() call's distance-field matrix into `out`."""
