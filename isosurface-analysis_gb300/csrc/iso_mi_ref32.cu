@@ -21,8 +21,8 @@
 // and their column and row sums (colrow: [2][m*m*bins]; exact integers, so
 // the histogram kernels' sums are the reference's).  One warp walks 32
 // pairs, one lane per pair: it stages 32 consecutive bins of each of its
-// pairs in shared memory with coalesced loads, then each lane continues its
-// pair's serial sum over the staged bins.  The row entropy is the sum over the
+// pairs in shared memory by asynchronous copies several steps ahead, and each
+// lane continues its pair's serial sum over the staged bins.  The row entropy is the sum over the
 // row sums in row order (the reference adds each at its row's end), the column
 // entropy over the column sums in column order.  The logarithm of a count
 // below 65536 is read from a table that logf_table_kernel fills with the
@@ -57,43 +57,80 @@ __device__ __forceinline__ float entropy_step(float h, uint32_t count, float lg)
     return h;
 }
 
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src, uint32_t src_bytes)
+{
+    // src_bytes 0: nothing is read and the 16 bytes are zero-filled
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Each step stages 32 bins of each of the CTA's 32 pairs (one 128-byte row
+// per pair, 4 KB) by asynchronous copies, R32_STAGES steps ahead of the walk,
+// so that the walk does not wait on memory.  A row's eight 16-byte chunks are
+// stored at chunk position c ^ (pair % 8), which lets the 32 lanes read their
+// own rows 16 bytes at a time without bank conflicts.  Bins past the
+// histogram's end are zero-filled: the walk skips zero counts, as the
+// reference does.
+constexpr int R32_STAGES = 6;
+
 __global__ void __launch_bounds__(R32_PAIRS) mi_ref32_kernel(const uint32_t *__restrict__ joint,
                                                             const uint32_t *__restrict__ colrow, int64_t num_pairs,
                                                             int bins, float num_values,
                                                             const float *__restrict__ logtab, float *__restrict__ ism)
 {
-    __shared__ uint32_t tile[R32_PAIRS * (R32_TILE + 1)];
+    static_assert(R32_TILE == 32 && R32_PAIRS == 32, "one 128-byte row per lane and step");
+    __shared__ __align__(16) uint32_t tiles[R32_STAGES][R32_PAIRS * R32_TILE];
     const int lane = threadIdx.x;
     const int64_t first = (int64_t)blockIdx.x * R32_PAIRS;
-    const int64_t hist = (int64_t)bins * bins;
+    const int64_t hist = (int64_t)bins * bins;  // a multiple of 4: bins is even
+    const int64_t steps = (hist + R32_TILE - 1) / R32_TILE;
+
+    // lane l copies chunk l % 8 of the rows of pairs 4 j + l / 8, j = 0..7
+    auto issue = [&](int64_t step, int st) {
+        if (step < steps) {
+            const int c = lane & 7;
+            const int64_t bin = step * R32_TILE + 4 * c;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int p = 4 * j + (lane >> 3);
+                const bool valid = first + p < num_pairs && bin < hist;
+                const uint32_t *src = valid ? joint + (first + p) * hist + bin : joint;
+                const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&tiles[st][p * R32_TILE + ((c ^ (p & 7)) << 2)]);
+                cp_async16(dst, src, valid ? 16u : 0u);
+            }
+        }
+        cp_async_commit();  // one group per step, empty past the end
+    };
+#pragma unroll
+    for (int s0 = 0; s0 < R32_STAGES - 1; ++s0) issue(s0, s0);
 
     float hXY = 0.0f;
-    for (int64_t k0 = 0; k0 < hist; k0 += R32_TILE) {
-        // stage bins k0 .. k0+31 of every pair of this CTA (128 B per pair)
-        const int64_t k = k0 + lane;
-#pragma unroll 8
-        for (int p = 0; p < R32_PAIRS; ++p) {
-            uint32_t v = 0;
-            if (first + p < num_pairs && k < hist) v = __ldcs(joint + (first + p) * hist + k);
-            tile[p * (R32_TILE + 1) + lane] = v;
-        }
+    for (int64_t step = 0; step < steps; ++step) {
+        const int st = (int)(step % R32_STAGES);
+        cp_async_wait<R32_STAGES - 2>();  // this step's copies (and every lane's: next line) have landed
         __syncwarp();
+        // the stage read in the previous step takes step + R32_STAGES - 1
+        issue(step + R32_STAGES - 1, (int)((step + R32_STAGES - 1) % R32_STAGES));
         // this lane's pair: the reference's row-major walk over the staged bins
-        const uint32_t *own = tile + lane * (R32_TILE + 1);
-        if (hist - k0 >= R32_TILE) {
+        const uint32_t *own = tiles[st] + lane * R32_TILE;
 #pragma unroll
-            for (int s = 0; s < R32_TILE; ++s) {
-                const uint32_t v = own[s];
-                if (v > 0) hXY = entropy_step(hXY, v, log_count(logtab, v));
-            }
-        } else {
-            for (int s = 0; s < (int)(hist - k0); ++s) {
-                const uint32_t v = own[s];
-                if (v > 0) hXY = entropy_step(hXY, v, log_count(logtab, v));
-            }
+        for (int q = 0; q < R32_TILE / 4; ++q) {
+            const uint4 v4 = *reinterpret_cast<const uint4 *>(own + ((q ^ (lane & 7)) << 2));
+            if (v4.x > 0) hXY = entropy_step(hXY, v4.x, log_count(logtab, v4.x));
+            if (v4.y > 0) hXY = entropy_step(hXY, v4.y, log_count(logtab, v4.y));
+            if (v4.z > 0) hXY = entropy_step(hXY, v4.z, log_count(logtab, v4.z));
+            if (v4.w > 0) hXY = entropy_step(hXY, v4.w, log_count(logtab, v4.w));
         }
-        __syncwarp();
+        __syncwarp();  // every lane is done with stage st before it is refilled
     }
+    cp_async_wait<0>();
     if (first + lane >= num_pairs) return;
     const uint32_t *cs = colrow + (first + lane) * bins;
     const uint32_t *rs = colrow + num_pairs * bins + (first + lane) * bins;

@@ -172,3 +172,21 @@ def test_config3_full_length_fields():
     assert np.array_equal(hrows.reshape(m * m, bins), rws)
     assert np.array_equal(hsim, sim)
     assert np.array_equal(ism32[np.ix_(rows, rows)], sim)
+
+
+@pytest.mark.parametrize("bins", [2, 6, 30])
+def test_few_bins(bins):
+    """Bin counts whose histograms end inside a 32-bin staging step of the
+    reference-order MI (4, 36 and 900 bins per pair): map and sums against the
+    reference kernel's, bit for bit."""
+    import isosim
+    rng = np.random.default_rng(bins)
+    n = 200003
+    base = rng.uniform(0, 1, n)
+    f = np.stack([np.abs(base * (1 + 0.2 * k) + 0.1 * rng.standard_normal(n)) for k in range(5)]).astype(np.float32)
+    sim, joint, cols, rows = refgpu.similarity(f, bins)
+    mins, maxs = f.min(axis=1), f.max(axis=1)
+    hsim, hcols, hrows = isosim.calculate_histogram_h(list(f), mins, maxs, bins)
+    assert np.array_equal(hcols.reshape(25, bins), cols)
+    assert np.array_equal(hrows.reshape(25, bins), rows)
+    assert np.array_equal(hsim, sim)
