@@ -425,6 +425,9 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
         // multiple of 32 words per row a warp covers part of one row, and a
         // warp sum replaces the per-thread row-sum atomics.
         const bool dump = a.joint_dump != nullptr;
+        // the transposed copy (pair (j, i)) is written column by column in a
+        // pass of its own, so the bin pass leaves the counters to it
+        const bool tdump = dump && a.symmetric && i != j;
         {
             const int groups = blockDim.x / wpr;
             const int w = threadIdx.x % wpr, g = threadIdx.x / wpr;
@@ -435,22 +438,16 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
                     const uint32_t word = words[r * wps + w];
                     uint32_t c0 = 0, c1 = 0;
                     if (word || dump) {
-                        words[r * wps + w] = 0;
+                        if (!tdump) words[r * wps + w] = 0;
                         c0 = word & 0xffffu;
                         c1 = word >> 16;
                         cs0 += c0;
                         cs1 += c1;
                         if (c0) hxy -= __ldg(a.clnc + c0);
                         if (c1) hxy -= __ldg(a.clnc + c1);
-                        if (dump) {
-                            const int c = 2 * w;
-                            a.joint_dump[(((size_t)i * a.m + j) * bins + r) * bins + c] = c0;
-                            a.joint_dump[(((size_t)i * a.m + j) * bins + r) * bins + c + 1] = c1;
-                            if (a.symmetric && i != j) {
-                                a.joint_dump[(((size_t)j * a.m + i) * bins + c) * bins + r] = c0;
-                                a.joint_dump[(((size_t)j * a.m + i) * bins + c + 1) * bins + r] = c1;
-                            }
-                        }
+                        if (dump)  // bins is even: 8-byte aligned, adjacent lanes adjacent
+                            *reinterpret_cast<uint2 *>(a.joint_dump + (((size_t)i * a.m + j) * bins + r) * bins +
+                                                       2 * w) = make_uint2(c0, c1);
                     }
                     if (warp_rows) {
                         const uint32_t rs = __reduce_add_sync(0xffffffffu, c0 + c1);
@@ -464,6 +461,20 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_mi_kernel(Pai
             }
         }
         __syncthreads();
+        if (tdump) {
+            // lanes take consecutive rows r of one counter-word column: two
+            // 128-byte stores per warp, and shared reads wps = bins/2 + 3
+            // words apart (odd for a multiple of 4 bins: conflict-free)
+            uint32_t *tj = a.joint_dump + ((size_t)j * a.m + i) * bins * bins;
+            for (int idx = threadIdx.x; idx < wpr * bins; idx += blockDim.x) {
+                const int w = idx / bins, r = idx - w * bins;
+                const uint32_t word = words[r * wps + w];
+                words[r * wps + w] = 0;
+                tj[(size_t)(2 * w) * bins + r] = word & 0xffffu;
+                tj[(size_t)(2 * w + 1) * bins + r] = word >> 16;
+            }
+            __syncthreads();  // the corrected bins below overwrite these
+        }
         if (dump && nev > 0) {
             // overwrite the corrected bins (distinct events carry c16 != or corr)
             for (int e = threadIdx.x; e < nev; e += blockDim.x) {
@@ -582,19 +593,17 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_wide_kernel(P
 
         // bins: sum(c ln c), marginals, optional dump; clears the counters
         const bool dump = a.joint_dump != nullptr;
+        const bool tdump = dump && a.symmetric && i != j;  // transposed copy: a pass of its own
         double hxy = 0.0;
         uint32_t cs = 0;
         for (int idx = threadIdx.x; idx < nb; idx += blockDim.x) {
             const int r = idx / bins, col = idx - r * bins;
             const uint32_t c = words[idx + r];  // padded row r starts at r * (bins + 1)
             if (c) {
-                words[idx + r] = 0;
+                if (!tdump) words[idx + r] = 0;
                 hxy -= clnc_of(a.clnc, c);
             }
-            if (dump) {
-                a.joint_dump[(((size_t)i * a.m + j) * bins + r) * bins + col] = c;
-                if (a.symmetric && i != j) a.joint_dump[(((size_t)j * a.m + i) * bins + col) * bins + r] = c;
-            }
+            if (dump) a.joint_dump[(((size_t)i * a.m + j) * bins + r) * bins + col] = c;
             if (warp_rows) {
                 const uint32_t rs = __reduce_add_sync(0xffffffffu, c);
                 if (lane == 0 && rs) atomicAdd(&s_rowsum[r], rs);
@@ -606,6 +615,17 @@ __global__ void __launch_bounds__(HIST_THREADS, 1) joint_histogram_wide_kernel(P
         }
         if (col_own && cs) atomicAdd(&s_colsum[threadIdx.x % bins], cs);
         __syncthreads();
+        if (tdump) {
+            // lanes take consecutive rows of one column: coalesced stores, and
+            // shared reads bins + 1 words apart
+            uint32_t *tj = a.joint_dump + ((size_t)j * a.m + i) * nb;
+            for (int idx = threadIdx.x; idx < nb; idx += blockDim.x) {
+                const int col = idx / bins, r = idx - col * bins;
+                tj[idx] = words[r * (bins + 1) + col];
+                words[r * (bins + 1) + col] = 0;
+            }
+            __syncthreads();
+        }
         double hx = 0.0, hy = 0.0;
         for (int c = threadIdx.x; c < bins; c += blockDim.x) {
             const unsigned long long cs64 = s_colsum[c], rs64 = s_rowsum[c];
