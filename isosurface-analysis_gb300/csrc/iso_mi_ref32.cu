@@ -27,7 +27,8 @@
 // entropy over the column sums in column order.  The logarithm of a count
 // below 65536 is read from a table that logf_table_kernel fills with the
 // device's own logf, so the serial chains carry only the fused
-// multiply-subtract.  The order of every summation chain is the reference's.
+// multiply-subtract, and a zero count's step leaves the sum unchanged, so the
+// walks have no branch per bin.  The order of every summation chain is the reference's.
 #include "iso_internal.cuh"
 
 namespace {
@@ -36,15 +37,26 @@ constexpr int R32_PAIRS = 32;        // ordered pairs per CTA (one warp, one lan
 constexpr int R32_TILE = 32;         // bins of each pair staged per step
 constexpr int R32_LOG_TABLE = 65536; // counts whose logarithm is tabulated
 
+// Entry 0 holds 0 rather than logf(0) = -inf: a zero count's step h - 0 * 0
+// then returns h unchanged (h is never -0: it starts at +0 and only falls),
+// which is what the reference's skip of zero counts does, and the walks below
+// need no branch per bin.
 __global__ void logf_table_kernel(float *t)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < R32_LOG_TABLE) t[c] = logf((float)c);
+    if (c < R32_LOG_TABLE) t[c] = c == 0 ? 0.0f : logf((float)c);
 }
 
 __device__ __forceinline__ float log_count(const float *__restrict__ tab, uint32_t c)
 {
     return c < (uint32_t)R32_LOG_TABLE ? __ldg(tab + c) : logf((float)c);
+}
+
+// The table entry of a count, clamped into the table (counts past it are
+// corrected by the caller).
+__device__ __forceinline__ float log_small(const float *__restrict__ tab, uint32_t c)
+{
+    return __ldg(tab + (c < (uint32_t)R32_LOG_TABLE ? c : (uint32_t)R32_LOG_TABLE - 1));
 }
 
 // The reference's per-bin term h -= c * logf(c) for a nonzero count, with
@@ -118,30 +130,50 @@ __global__ void __launch_bounds__(R32_PAIRS) mi_ref32_kernel(const uint32_t *__r
         __syncwarp();
         // the stage read in the previous step takes step + R32_STAGES - 1
         issue(step + R32_STAGES - 1, (int)((step + R32_STAGES - 1) % R32_STAGES));
-        // this lane's pair: the reference's row-major walk over the staged bins
+        // this lane's pair: the reference's row-major walk over the staged
+        // bins.  Counts and logarithms of all 32 bins are fetched before the
+        // chain, with no branch between them; zero counts step through the
+        // chain unchanged (table entry 0).
         const uint32_t *own = tiles[st] + lane * R32_TILE;
+        uint32_t v[R32_TILE];
 #pragma unroll
         for (int q = 0; q < R32_TILE / 4; ++q) {
             const uint4 v4 = *reinterpret_cast<const uint4 *>(own + ((q ^ (lane & 7)) << 2));
-            if (v4.x > 0) hXY = entropy_step(hXY, v4.x, log_count(logtab, v4.x));
-            if (v4.y > 0) hXY = entropy_step(hXY, v4.y, log_count(logtab, v4.y));
-            if (v4.z > 0) hXY = entropy_step(hXY, v4.z, log_count(logtab, v4.z));
-            if (v4.w > 0) hXY = entropy_step(hXY, v4.w, log_count(logtab, v4.w));
+            v[4 * q] = v4.x;
+            v[4 * q + 1] = v4.y;
+            v[4 * q + 2] = v4.z;
+            v[4 * q + 3] = v4.w;
         }
         __syncwarp();  // every lane is done with stage st before it is refilled
+        float lg[R32_TILE];
+        uint32_t any = 0;
+#pragma unroll
+        for (int k = 0; k < R32_TILE; ++k) {
+            lg[k] = log_small(logtab, v[k]);
+            any |= v[k];
+        }
+        if (any >= (uint32_t)R32_LOG_TABLE) {
+#pragma unroll
+            for (int k = 0; k < R32_TILE; ++k)
+                if (v[k] >= (uint32_t)R32_LOG_TABLE) lg[k] = logf((float)v[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < R32_TILE; ++k) hXY = entropy_step(hXY, v[k], lg[k]);
     }
     cp_async_wait<0>();
     if (first + lane >= num_pairs) return;
     const uint32_t *cs = colrow + (first + lane) * bins;
     const uint32_t *rs = colrow + num_pairs * bins + (first + lane) * bins;
-    float hX = 0.0f, hY = 0.0f;
+    float hX = 0.0f, hY = 0.0f;  // zero sums step through unchanged, as above
+#pragma unroll 8
     for (int c = 0; c < bins; ++c) {
         const uint32_t v = __ldg(cs + c);
-        if (v > 0) hX = entropy_step(hX, v, log_count(logtab, v));
+        hX = entropy_step(hX, v, log_count(logtab, v));
     }
+#pragma unroll 8
     for (int r = 0; r < bins; ++r) {
         const uint32_t v = __ldg(rs + r);
-        if (v > 0) hY = entropy_step(hY, v, log_count(logtab, v));
+        hY = entropy_step(hY, v, log_count(logtab, v));
     }
     // JointHistogram.cu:53-59, operation for operation
     hXY = hXY / num_values + logf(num_values);
