@@ -142,18 +142,25 @@ __device__ __forceinline__ void bins4(const Binner &bn, const float4 &x, const f
         const float2 hy01 = __ffma2_ru(dy01, nrh, nb), hy23 = __ffma2_ru(dy23, nrh, nb);
         const float2 zx01 = __fadd2_rn(lx01, hx01), zx23 = __fadd2_rn(lx23, hx23);
         const float2 zy01 = __fadd2_rn(ly01, hy01), zy23 = __fadd2_rn(ly23, hy23);
-        // bucket = min(bits(lo) - bits(2^23), bins - 1) as unsigned: any input
-        // (also one outside the interval) stays inside the histogram
+        // bucket = bits(lo) - bits(2^23).  The generic instance (FB == 0)
+        // clamps it to bins - 1 as unsigned, so that any input (also one above
+        // a caller's interval) stays inside the histogram.  The specialised
+        // instances run only where every value v lies in its pair's interval
+        // (the dispatch picks the generic one otherwise), and there no clamp
+        // is needed: d = RN(v - mn) <= RN(mx - mn) = range, and with
+        // step = RN(range / bins) >= (range / bins)(1 - 2^-24) and
+        // r <= (1 / step)(1 + 2^-24), range * rlo <= bins (1 + 2^-24)
+        // (1 - 2^-22) / (1 - 2^-24) < bins, so lo < 2^23 + bins.
         const uint32_t top = (uint32_t)(bins - 1);
         const uint32_t ub = (uint32_t)rstride;
-        b0 = (int)(min(__float_as_uint(lx01.x) - FLOOR_BASE_BITS, top) * ub +
-                   min(__float_as_uint(ly01.x) - FLOOR_BASE_BITS, top));
-        b1 = (int)(min(__float_as_uint(lx01.y) - FLOOR_BASE_BITS, top) * ub +
-                   min(__float_as_uint(ly01.y) - FLOOR_BASE_BITS, top));
-        b2 = (int)(min(__float_as_uint(lx23.x) - FLOOR_BASE_BITS, top) * ub +
-                   min(__float_as_uint(ly23.x) - FLOOR_BASE_BITS, top));
-        b3 = (int)(min(__float_as_uint(lx23.y) - FLOOR_BASE_BITS, top) * ub +
-                   min(__float_as_uint(ly23.y) - FLOOR_BASE_BITS, top));
+        auto bucket = [&](float lo) {
+            const uint32_t b = __float_as_uint(lo) - FLOOR_BASE_BITS;
+            return FB ? b : min(b, top);
+        };
+        b0 = (int)(bucket(lx01.x) * ub + bucket(ly01.x));
+        b1 = (int)(bucket(lx01.y) * ub + bucket(ly01.y));
+        b2 = (int)(bucket(lx23.x) * ub + bucket(ly23.x));
+        b3 = (int)(bucket(lx23.y) * ub + bucket(ly23.y));
         const bool slow = ((__float_as_uint(zx01.x) | __float_as_uint(zx01.y) | __float_as_uint(zx23.x) |
                             __float_as_uint(zx23.y) | __float_as_uint(zy01.x) | __float_as_uint(zy01.y) |
                             __float_as_uint(zy23.x) | __float_as_uint(zy23.y)) != 0u);
@@ -339,7 +346,8 @@ __device__ __forceinline__ Binner make_binner(const uint32_t *mma, const uint32_
     // mode 0 needs a finite interval (every non-NaN value then lies in it) and
     // a normal, finite step with finite nonzero reciprocals
     bn.mode = bn.step == 0.0f ? 2
-              : (isfinite(bn.step) && bn.step >= 1.17549435e-38f && isfinite(r) && r > 0.0f && isfinite(bn.rhi)
+              : (isfinite(bn.step) && bn.step >= 1.17549435e-38f && isfinite(r) && r >= 1.17549435e-38f &&
+                         isfinite(bn.rhi)
                      ? 0
                      : 1);
     return bn;
@@ -1098,17 +1106,21 @@ __global__ void __launch_bounds__(MI_THREADS) joint_mi_kernel(MiArgs a)
 // stride as constants in the streaming loop), else the generic instance.
 using PairKernel = void (*)(PairArgs);
 using SegKernel = void (*)(SegArgs);
-PairKernel mi_kernel_for(int bins)
+// clamp: some value lies above its pair's interval (only the generic
+// instances clamp the fast path's buckets).
+PairKernel mi_kernel_for(int bins, bool clamp)
 {
-    return bins == 256 ? joint_histogram_mi_kernel<256, false, false> : joint_histogram_mi_kernel<0, false, false>;
+    return bins == 256 && !clamp ? joint_histogram_mi_kernel<256, false, false>
+                                 : joint_histogram_mi_kernel<0, false, false>;
 }
-PairKernel wide_kernel_for(int bins)
+PairKernel wide_kernel_for(int bins, bool clamp)
 {
-    return bins == 128 ? joint_histogram_wide_kernel<128> : joint_histogram_wide_kernel<0>;
+    return bins == 128 && !clamp ? joint_histogram_wide_kernel<128> : joint_histogram_wide_kernel<0>;
 }
-SegKernel seg_kernel_for(int bins)
+SegKernel seg_kernel_for(int bins, bool clamp)
 {
-    return bins == 256 ? joint_histogram_seg_kernel<256, true, true> : joint_histogram_seg_kernel<0, true, true>;
+    return bins == 256 && !clamp ? joint_histogram_seg_kernel<256, true, true>
+                                 : joint_histogram_seg_kernel<0, true, true>;
 }
 
 __global__ void clnc_table_kernel(double *table)
@@ -1293,7 +1305,7 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
         // long fields, packed counters: segment-major schedule, pairs in chunks
         // bounding the global histograms to ISO_HIST_CHUNK_BYTES (and the task
         // count to int range)
-        const SegKernel seg_kernel = seg_kernel_for(bins);
+        const SegKernel seg_kernel = seg_kernel_for(bins, ctx->hist_clamp_top);
         ISO_CUDA(cudaFuncSetAttribute(seg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)(packed_words(ISO_MAX_BINS) * sizeof(uint32_t))));
         const size_t hist_bytes = (size_t)bins * bins * sizeof(uint32_t);
@@ -1381,7 +1393,7 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
     if (bins <= WIDE_MAX_BINS) {
         // 32-bit counters: no wrap events
         const size_t wsmem = (size_t)wide_words(bins) * sizeof(uint32_t);
-        const PairKernel wide_kernel = wide_kernel_for(bins);
+        const PairKernel wide_kernel = wide_kernel_for(bins, ctx->hist_clamp_top);
         ISO_CUDA(cudaFuncSetAttribute(wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)(wide_words(WIDE_MAX_BINS) * sizeof(uint32_t))));
         int per_sm_w = 0;
@@ -1413,7 +1425,7 @@ int iso_run_similarity_tasks(iso_ctx *ctx, const float *d_fields_a, const float 
         ISO_LAUNCHED(ctx);
         return ISO_OK;
     }
-    const PairKernel mi_kernel = mi_kernel_for(bins);
+    const PairKernel mi_kernel = mi_kernel_for(bins, ctx->hist_clamp_top);
     ISO_CUDA(cudaFuncSetAttribute(mi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)(packed_words(ISO_MAX_BINS) * sizeof(uint32_t))));
     int per_sm = 0;
@@ -1522,11 +1534,11 @@ int noalloc_setup(int device, NoAllocDevice **out)
             return iso_fail(ISO_ERR_CUDA, "iso_similarity_map_noalloc: cudaGetSymbolAddress failed: %s",
                             cudaGetErrorString(e));
         for (int b : {0, 256})
-            ISO_CUDA(cudaFuncSetAttribute(mi_kernel_for(b), cudaFuncAttributeMaxDynamicSharedMemorySize,
+            ISO_CUDA(cudaFuncSetAttribute(mi_kernel_for(b, false), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)(packed_words(ISO_MAX_BINS) * sizeof(uint32_t))));
         int sms = 0, per_sm = 0;
         ISO_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-        ISO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mi_kernel_for(0), HIST_THREADS,
+        ISO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mi_kernel_for(0, false), HIST_THREADS,
                                                                packed_words(ISO_MAX_BINS) * sizeof(uint32_t)));
         int grid = sms * (per_sm < 1 ? 1 : per_sm);
         d.grid = grid < NOALLOC_MAX_CTAS ? grid : NOALLOC_MAX_CTAS;
@@ -1608,7 +1620,7 @@ extern "C" int iso_similarity_map_noalloc(const float *d_fields, int m, int64_t 
     a.colrow_dump = nullptr;
     const int grid = d->grid < num_tasks ? d->grid : num_tasks;
     const size_t smem = (size_t)packed_words(bins) * sizeof(uint32_t);
-    mi_kernel_for(bins)<<<grid, HIST_THREADS, smem, st>>>(a);
+    mi_kernel_for(bins, false)<<<grid, HIST_THREADS, smem, st>>>(a);  // intervals of its own fields
     ISO_CUDA(cudaGetLastError());
     int err = 0;
     ISO_CUDA(cudaMemcpyAsync(&err, ctrl + 1, sizeof(int), cudaMemcpyDeviceToHost, st));

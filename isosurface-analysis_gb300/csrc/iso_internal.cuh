@@ -118,6 +118,9 @@ struct iso_ctx {
     int64_t device_bytes_cap = 0;  // ISO_LIMIT_DEVICE_BYTES (0: none)
     int query_run = 0;             // ISO_LIMIT_QUERY_RUN (0: by volume size)
     int hist_row_codes = 0;        // ISO_LIMIT_HIST_ROW_CODES
+    // set while a caller-supplied interval leaves values of its field above
+    // its maximum: the histogram kernels must then clamp buckets to the last bin
+    bool hist_clamp_top = false;
     // joint histograms of all ordered pairs kept in BUF_HIST_DUMP by the last
     // ISO_MI_REF32 similarity run (0 = none)
     int joint_m = 0, joint_bins = 0;

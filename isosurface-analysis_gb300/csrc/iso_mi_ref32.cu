@@ -29,6 +29,7 @@
 // device's own logf, so the serial chains carry only the fused
 // multiply-subtract, and a zero count's step leaves the sum unchanged, so the
 // walks have no branch per bin.  The order of every summation chain is the reference's.
+#include "iso_async.cuh"
 #include "iso_internal.cuh"
 
 namespace {
@@ -67,20 +68,6 @@ __device__ __forceinline__ float entropy_step(float h, uint32_t count, float lg)
     float c = (float)count;
     h -= c * lg;
     return h;
-}
-
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src, uint32_t src_bytes)
-{
-    // src_bytes 0: nothing is read and the 16 bytes are zero-filled
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
-}
-
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-
-template <int N>
-__device__ __forceinline__ void cp_async_wait()
-{
-    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 // Each step stages 32 bins of each of the CTA's 32 pairs (one 128-byte row

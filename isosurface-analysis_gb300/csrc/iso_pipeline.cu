@@ -322,6 +322,7 @@ static int similarity_impl(iso_ctx *ctx, const float *const *field_ptrs, const f
     ISO_TRY(iso_buf(ctx, BUF_FIELD_MINMAX, (size_t)2 * nf * sizeof(uint32_t), &d_mm));
     ISO_TRY(iso_buf(ctx, BUF_ISM, (size_t)m * m * sizeof(float), &d_ism));
     float *f = (float *)d_fields;
+    bool clamp_top = false;  // a caller's interval leaves values above its maximum
     if (field_ptrs) {
         for (int k = 0; k < nf; ++k)
             ISO_CUDA(cudaMemcpyAsync(f + (size_t)k * stride, field_ptrs[k], (size_t)n * sizeof(float), cudaMemcpyDefault,
@@ -343,6 +344,7 @@ static int similarity_impl(iso_ctx *ctx, const float *const *field_ptrs, const f
         ISO_CUDA(cudaMemcpy(hmin.data(), mins, nf * sizeof(float), cudaMemcpyDefault));
         ISO_CUDA(cudaMemcpy(hmax.data(), maxs, nf * sizeof(float), cudaMemcpyDefault));
         ISO_CUDA(cudaStreamSynchronize(ctx->stream));
+        clamp_top = false;
         for (int k = 0; k < nf; ++k) {
             float lo, hi;
             memcpy(&lo, &mm[2 * k], sizeof lo);
@@ -350,7 +352,7 @@ static int similarity_impl(iso_ctx *ctx, const float *const *field_ptrs, const f
             if (!(hmin[k] <= lo) || !(hmax[k] >= hmin[k]))
                 return iso_fail(ISO_ERR_ARG, "field %d: interval [%g, %g] is empty or above its smallest value %g", k,
                                 hmin[k], hmax[k], lo);
-            (void)hi;
+            if (hi > hmax[k]) clamp_top = true;
         }
         void *d_tmp;
         ISO_TRY(iso_buf(ctx, BUF_STAGING_B, (size_t)2 * nf * sizeof(float), &d_tmp));
@@ -363,6 +365,11 @@ static int similarity_impl(iso_ctx *ctx, const float *const *field_ptrs, const f
         ISO_TRY(iso_run_minmax(ctx, f, nf, n, stride, (uint32_t *)d_mm));
     }
     uint32_t *d_joint = nullptr, *d_cr = nullptr;
+    struct ClampScope {  // the histogram kernels clamp only for this call
+        iso_ctx *c;
+        ~ClampScope() { c->hist_clamp_top = false; }
+    } clamp_scope{ctx};
+    ctx->hist_clamp_top = clamp_top;
     if (joint_out) {
         void *p;
         ISO_TRY(iso_buf(ctx, BUF_HIST_DUMP, (size_t)m * m * bins * bins * sizeof(uint32_t), &p));
