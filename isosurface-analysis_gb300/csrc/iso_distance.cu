@@ -134,8 +134,8 @@ struct Bvh {
     float4 *compact;         // gathered points, compact numbering
     float4 *leaves;          // sorted points
     BvhNode *nodes;          // segment s owns nodes [cstart[s]-s, cstart[s]-s+count-1)
-    int *parent_node;        // per internal node: parent*2 + side, -1 at the root
-    unsigned int *flags;
+    int *parent_node;        // per internal node: parent (group-wide index)*4 + side*2 + parent local, -1 at the root
+    unsigned int *flags;     // per internal node: leaf children (count | left << 8 | right << 9), then arrivals
     int *error;
 };
 
@@ -177,9 +177,20 @@ __device__ __forceinline__ void store_box(BvhNode *node, int side, float3 lo, fl
     __stcg(c + 2 + side, -hi.z);
 }
 
+// Block size of bvh_boxes_kernel, one thread per internal node.  A node whose
+// subtree's internal nodes all fall into one block of BOX_THREADS node
+// indices is "local": every arrival at it comes from that block.
+constexpr int BOX_THREADS = 256;
+// Points of one LBVH build (the parent links hold group-wide node indices * 4).
+constexpr int64_t LBVH_MAX_GROUP_POINTS = (int64_t)1 << 29;
+
 // One thread per internal node (Karras split).  Leaf children's boxes (their
 // points) are written here, and each node's arrival flag starts at its number
-// of leaf children, so the box pass starts at the nodes with two leaves.
+// of leaf children, so the box pass starts at the nodes with two leaves.  The
+// internal nodes of a subtree over leaves [first, last] have indices in
+// [first, last] (each node's index is an end of its own range), so the node is
+// local when nbase + first and nbase + last fall into one block; the flag goes
+// into its children's parent links.
 __global__ void bvh_build_kernel(Bvh b, const unsigned long long *sorted_keys)
 {
     int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -235,10 +246,12 @@ __global__ void bvh_build_kernel(Bvh b, const unsigned long long *sorted_keys)
         const float4 q = lv[right & ~LEAF_BIT];
         store_box(node, 1, make_float3(q.x, q.y, q.z), make_float3(q.x, q.y, q.z));
     }
-    node->d = make_int4(left, right, 0, 0);
-    b.flags[nbase + i] = (unsigned int)ll + (unsigned int)rl;
-    if (!ll) b.parent_node[nbase + left] = i * 2 + 0;
-    if (!rl) b.parent_node[nbase + right] = i * 2 + 1;
+    const int local = (nbase + first) / BOX_THREADS == (nbase + last) / BOX_THREADS ? 1 : 0;
+    node->d = make_int4(left, right, local, 0);
+    b.flags[nbase + i] = ((unsigned int)ll + (unsigned int)rl) | ((unsigned int)ll << 8) | ((unsigned int)rl << 9);
+    const int self = (int)(nbase + i) * 4 + local;  // group-wide index: below 2^29
+    if (!ll) b.parent_node[nbase + left] = self + 0;
+    if (!rl) b.parent_node[nbase + right] = self + 2;
     if (i == 0) b.parent_node[nbase] = -1;
 }
 
@@ -252,38 +265,99 @@ __device__ __forceinline__ unsigned int arrive_acq_rel(unsigned int *p)
     return old;
 }
 
-// Bottom-up boxes, one thread per internal node with two leaf children (its
-// box is complete after bvh_build_kernel).  A thread stores its node's box
-// into the parent and arrives there; the parent's flag counts leaf children
-// plus arrivals, so the thread that brings it to 2 carries on upwards.
-__global__ void bvh_boxes_kernel(Bvh b)
+// The same at block scope, on a flag in shared memory.
+__device__ __forceinline__ unsigned int arrive_acq_rel_cta(unsigned int *p)
 {
-    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= b.total - b.m) return;
-    const int4 cd = b.nodes[g].d;
-    if (!((cd.x & LEAF_BIT) && (cd.y & LEAF_BIT))) return;
-    int lo_s = 0, hi_s = b.m - 1;  // the segment owning node g (as in bvh_build_kernel)
-    while (lo_s < hi_s) {
-        const int mid = (lo_s + hi_s + 1) >> 1;
-        if (b.cstart[mid] - mid <= g) lo_s = mid; else hi_s = mid - 1;
+    unsigned int old;
+    asm volatile("atom.acq_rel.cta.shared::cta.add.u32 %0, [%1], 1;"
+                 : "=r"(old)
+                 : "r"((uint32_t)__cvta_generic_to_shared(p))
+                 : "memory");
+    return old;
+}
+
+// Bottom-up boxes, one thread per internal node.  The climb starts at the
+// nodes with two leaf children (their boxes are complete after
+// bvh_build_kernel): a thread writes its node's box into the parent's half
+// and arrives there; the parent's flag counts leaf children plus arrivals,
+// so the thread that brings it to 2 carries on upwards with the union of its
+// box and the sibling's.
+//
+// Phase 1, local parents (every arrival from this block): the block's nodes,
+// flags and links are loaded into shared memory first (coalesced), and the
+// climb runs there, ordered by the block barrier's successor, a block-scope
+// acquire-release on the shared flag, with no global access.  The local nodes
+// whose boxes changed are then written back in one coalesced pass.  Phase 2,
+// the remaining climbs (parents whose subtrees span blocks): boxes and flags
+// in global memory, ordered at device scope.
+__global__ void __launch_bounds__(BOX_THREADS) bvh_boxes_kernel(Bvh b)
+{
+    __shared__ unsigned int s_flag[BOX_THREADS];
+    __shared__ int s_link[BOX_THREADS];
+    __shared__ float4 s_node[BOX_THREADS][3];  // a, b, c of the block's nodes
+    const int64_t total_nodes = b.total - b.m;
+    const int64_t base = (int64_t)blockIdx.x * BOX_THREADS;
+    const int64_t g = base + threadIdx.x;
+    int4 cd = make_int4(0, 0, 0, 0);
+    if (g < total_nodes) {
+        s_flag[threadIdx.x] = b.flags[g];
+        s_link[threadIdx.x] = b.parent_node[g];
+        s_node[threadIdx.x][0] = __ldcg(&b.nodes[g].a);
+        s_node[threadIdx.x][1] = __ldcg(&b.nodes[g].b);
+        s_node[threadIdx.x][2] = __ldcg(&b.nodes[g].c);
+        cd = b.nodes[g].d;
     }
-    const int64_t nbase = b.cstart[lo_s] - lo_s;
-    const float4 ga = __ldcg(&b.nodes[g].a), gb = __ldcg(&b.nodes[g].b), gc = __ldcg(&b.nodes[g].c);
-    float3 lo = make_float3(fminf(ga.x, ga.y), fminf(ga.z, ga.w), fminf(gb.x, gb.y));
-    float3 hi = make_float3(-fminf(gb.z, gb.w), -fminf(gc.x, gc.y), -fminf(gc.z, gc.w));
-    int link = b.parent_node[g];
-    // depth is bounded by the 62-bit augmented key, the loop by the node count
-    for (int guard = 0; guard < 4096 && link >= 0; ++guard) {
-        const int parent = link >> 1, side = link & 1;
-        BvhNode *node = b.nodes + nbase + parent;
+    __syncthreads();
+    bool climbing = g < total_nodes && (cd.x & LEAF_BIT) && (cd.y & LEAF_BIT);
+    float3 lo = make_float3(0.f, 0.f, 0.f), hi = lo;
+    int link = -1;
+    if (climbing) {
+        const float4 ga = s_node[threadIdx.x][0], gb = s_node[threadIdx.x][1], gc = s_node[threadIdx.x][2];
+        lo = make_float3(fminf(ga.x, ga.y), fminf(ga.z, ga.w), fminf(gb.x, gb.y));
+        hi = make_float3(-fminf(gb.z, gb.w), -fminf(gc.x, gc.y), -fminf(gc.z, gc.w));
+        link = s_link[threadIdx.x];
+    }
+    // depth is bounded by the 62-bit augmented key, the loops by the node count
+    int guard = 0;
+    for (; climbing && link >= 0 && (link & 1) && guard < 4096; ++guard) {
+        const int t = (link >> 2) - (int)base, side = (link >> 1) & 1;  // parent inside this block
+        if ((unsigned int)t >= (unsigned int)BOX_THREADS) {  // a local parent outside the block: a build error
+            atomicExch(b.error, 1);
+            climbing = false;
+            break;
+        }
+        float *half = &s_node[t][0].x;
+        half[side] = lo.x, half[2 + side] = lo.y, half[4 + side] = lo.z;
+        half[6 + side] = -hi.x, half[8 + side] = -hi.y, half[10 + side] = -hi.z;
+        if ((arrive_acq_rel_cta(&s_flag[t]) & 0xffu) == 0) {
+            climbing = false;  // sibling not done yet
+            break;
+        }
+        const float4 na = s_node[t][0], nb = s_node[t][1], nc = s_node[t][2];
+        lo = make_float3(fminf(na.x, na.y), fminf(na.z, na.w), fminf(nb.x, nb.y));
+        hi = make_float3(-fminf(nb.z, nb.w), -fminf(nc.x, nc.y), -fminf(nc.z, nc.w));
+        link = s_link[t];
+    }
+    __syncthreads();
+    // write back the local nodes with an internal child (the others are
+    // unchanged, and a spanning node's halves live in global memory)
+    if (g < total_nodes && cd.z && !((cd.x & LEAF_BIT) && (cd.y & LEAF_BIT))) {
+        __stcg(&b.nodes[g].a, s_node[threadIdx.x][0]);
+        __stcg(&b.nodes[g].b, s_node[threadIdx.x][1]);
+        __stcg(&b.nodes[g].c, s_node[threadIdx.x][2]);
+    }
+    for (; climbing && link >= 0 && guard < 4096; ++guard) {
+        const int64_t pg = link >> 2;
+        const int side = (link >> 1) & 1;
+        BvhNode *node = b.nodes + pg;
         store_box(node, side, lo, hi);
-        if (arrive_acq_rel(&b.flags[nbase + parent]) == 0) return;  // sibling not done yet
+        if ((arrive_acq_rel(&b.flags[pg]) & 0xffu) == 0) return;  // sibling not done yet
         const float4 na = __ldcg(&node->a), nb = __ldcg(&node->b), nc = __ldcg(&node->c);
         lo = make_float3(fminf(na.x, na.y), fminf(na.z, na.w), fminf(nb.x, nb.y));
         hi = make_float3(-fminf(nb.z, nb.w), -fminf(nc.x, nc.y), -fminf(nc.z, nc.w));
-        link = b.parent_node[nbase + parent];
+        link = b.parent_node[pg];
     }
-    if (link >= 0) atomicExch(b.error, 1);
+    if (climbing && link >= 0) atomicExch(b.error, 1);
 }
 
 __device__ __forceinline__ float max3f(float a, float b, float c)
@@ -568,6 +642,8 @@ static int lbvh_group(iso_ctx *ctx, const SampleGrid &g, Segments sg, const int6
         cstart[q] = total;
         total += h_count[q];
     }
+    if (total >= LBVH_MAX_GROUP_POINTS)  // parent links hold the node index * 4
+        return iso_fail(ISO_ERR_CAPACITY, "surface %d has too many points (%lld)", seg0, (long long)total);
     if (total >= (int64_t)0x7fffffff) return iso_fail(ISO_ERR_CAPACITY, "too many surface points (%lld)", (long long)total);
     void *d_cstart, *d_keys, *d_keys2, *d_vals, *d_vals2, *d_compact, *d_leaves, *d_nodes, *d_pn, *d_flags, *d_misc;
     ISO_TRY(iso_buf(ctx, BUF_STAGING_A, (size_t)m * 2 * sizeof(int64_t), &d_cstart));
@@ -623,7 +699,7 @@ static int lbvh_group(iso_ctx *ctx, const SampleGrid &g, Segments sg, const int6
     if (total_nodes > 0) {
         bvh_build_kernel<<<(unsigned)((total_nodes + 255) / 256), 256, 0, ctx->stream>>>(b, kb.Current());
         ISO_LAUNCHED(ctx);
-        bvh_boxes_kernel<<<(unsigned)((total_nodes + 255) / 256), 256, 0, ctx->stream>>>(b);
+        bvh_boxes_kernel<<<(unsigned)((total_nodes + BOX_THREADS - 1) / BOX_THREADS), BOX_THREADS, 0, ctx->stream>>>(b);
         ISO_LAUNCHED(ctx);
     }
     for (int base = 0; base < m; base += 65535) {
@@ -708,7 +784,9 @@ int iso_run_distance(iso_ctx *ctx, int X, int Y, int Z, int ds, int method, cons
         for (int q0 = 0; q0 < m;) {
             int q1 = q0;
             int64_t pts = 0;
-            while (q1 < m && (q1 == q0 || pts + h_seg_count[q1] <= ctx->lbvh_group_points)) pts += h_seg_count[q1++];
+            const int64_t cap = ctx->lbvh_group_points < LBVH_MAX_GROUP_POINTS - 1 ? ctx->lbvh_group_points
+                                                                                   : LBVH_MAX_GROUP_POINTS - 1;
+            while (q1 < m && (q1 == q0 || pts + h_seg_count[q1] <= cap)) pts += h_seg_count[q1++];
             ISO_TRY(lbvh_group(ctx, g, sg, h_seg_count + q0, q1 - q0, q0, fields + (size_t)q0 * field_stride,
                                field_stride));
             q0 = q1;
