@@ -352,6 +352,30 @@ def test_values_above_caller_maxima_256_bins(n):
     assert above > 0
 
 
+@pytest.mark.parametrize("n,bins", [(300001, 256), (2500003, 256), (70001, 128)])
+def test_caller_intervals_wider_than_values(n, bins):
+    """Caller-supplied intervals that contain every value, some wider than
+    the field's own (lower minima, higher maxima): the 256- and 128-bin
+    kernel instances then skip the fast path's bucket clamp.  Column and row
+    sums bit-exact against the oracle with the same intervals, in the fused
+    (300,001 and 70,001 values) and segment-major (2,500,003) kernels."""
+    import isosim
+    m = 4
+    fields = list(fields_like_df(m, n, seed=n % 997 + bins))
+    mins, maxs = [], []
+    for k, f in enumerate(fields):
+        lo, hi = oracle.field_interval(f)
+        widen = 0.0 if k == 0 else 0.05 * k * (hi - lo)  # field 0 keeps its own interval
+        mins.append(float(np.float32(lo - widen)))
+        maxs.append(float(np.float32(hi + widen)))
+    sim, cols, rows = isosim.calculate_histogram_h(fields, mins, maxs, bins)
+    for i in range(m):
+        for j in range(m):
+            joint, cs, rs = oracle.pair_histogram(fields[i], fields[j], bins, (mins[i], maxs[i]), (mins[j], maxs[j]))
+            assert np.array_equal(cols[i, j], cs) and np.array_equal(rows[i, j], rs), (i, j)
+            assert abs(sim[i, j] - oracle.mi_f32(joint, cs, rs, n)) < TOL_REF_HOST
+
+
 def test_values_below_caller_minimum_refused():
     """A caller-supplied minimum above one of its field's values is refused
     (the reference would index below its histogram)."""
