@@ -95,8 +95,9 @@ struct BvhNode {
 };
 constexpr int LEAF_BIT = (int)0x80000000;
 
-// Expands a 10-bit integer into 30 bits with two zeros between bits and the
-// 30-bit Morton code of a point in the unit cube, as BVH.cu:84-117 computes it.
+// Expands a 10-bit integer into 30 bits with two zeros between bits, and the
+// Morton code of a point in the unit cube with `bits` bits per axis (at most
+// 10; with 10 it is the 30-bit code of BVH.cu:84-117).
 __device__ __forceinline__ unsigned int expand_bits(unsigned int v)
 {
     v = (v * 0x00010001u) & 0xFF0000FFu;
@@ -106,12 +107,31 @@ __device__ __forceinline__ unsigned int expand_bits(unsigned int v)
     return v;
 }
 
-__device__ __forceinline__ unsigned int morton30(float x, float y, float z)
+__device__ __forceinline__ unsigned int morton_code(float x, float y, float z, int bits)
 {
-    x = fminf(fmaxf(__fmul_rn(x, 1024.0f), 0.0f), 1023.0f);
-    y = fminf(fmaxf(__fmul_rn(y, 1024.0f), 0.0f), 1023.0f);
-    z = fminf(fmaxf(__fmul_rn(z, 1024.0f), 0.0f), 1023.0f);
+    const float cells = (float)(1u << bits), top = cells - 1.0f;
+    x = fminf(fmaxf(__fmul_rn(x, cells), 0.0f), top);
+    y = fminf(fmaxf(__fmul_rn(y, cells), 0.0f), top);
+    z = fminf(fmaxf(__fmul_rn(z, cells), 0.0f), top);
     return expand_bits((unsigned int)x) * 4 + expand_bits((unsigned int)y) * 2 + expand_bits((unsigned int)z);
+}
+
+// Sort keys of one LBVH group: the surface index in the top seg_bits bits and
+// the point's Morton code below, with as many bits per axis as fit in 32 (10
+// for up to 4 surfaces, 8 for up to 256, the most a group holds).  Coarser
+// codes only loosen the lowest boxes; the queries' minima are exact whatever
+// the tree.
+constexpr int LBVH_MAX_GROUP_SURFACES = 256;
+inline int lbvh_seg_bits(int m)
+{
+    int b = 0;
+    while ((1 << b) < m) ++b;
+    return b;
+}
+inline int lbvh_axis_bits(int m)
+{
+    const int a = (32 - lbvh_seg_bits(m)) / 3;
+    return a < 10 ? a : 10;
 }
 
 __device__ __forceinline__ int find_segment(const int64_t *starts, int m, int64_t i)
@@ -129,7 +149,8 @@ struct Bvh {
     const int64_t *ccount;   // per segment: leaves
     int m;
     int64_t total;           // all leaves
-    unsigned long long *keys;
+    unsigned int *keys;      // surface index above the Morton code (lbvh_axis_bits)
+    int axis_bits;
     unsigned int *vals;
     float4 *compact;         // gathered points, compact numbering
     float4 *leaves;          // sorted points
@@ -146,7 +167,7 @@ __global__ void bvh_keys_kernel(Segments sg, Bvh b)
     int s = find_segment(b.cstart, b.m, i);
     float4 p = sg.points[sg.offset[s] + (i - b.cstart[s])];
     b.compact[i] = p;
-    b.keys[i] = ((unsigned long long)s << 32) | morton30(p.x, p.y, p.z);
+    b.keys[i] = ((unsigned int)s << (3 * b.axis_bits)) | morton_code(p.x, p.y, p.z, b.axis_bits);
     b.vals[i] = (unsigned int)i;
 }
 
@@ -158,10 +179,10 @@ __global__ void bvh_gather_kernel(Bvh b, const unsigned int *sorted_vals)
 }
 
 // delta of the Karras construction over index-augmented keys
-__device__ __forceinline__ int karras_delta(const unsigned long long *codes, int n, int i, int j)
+__device__ __forceinline__ int karras_delta(const unsigned int *codes, int n, int i, int j)
 {
     if (j < 0 || j >= n) return -1;
-    unsigned int ci = (unsigned int)codes[i], cj = (unsigned int)codes[j];
+    const unsigned int ci = codes[i], cj = codes[j];
     if (ci == cj) return 32 + __clz(i ^ j);
     return __clz(ci ^ cj);
 }
@@ -191,7 +212,7 @@ constexpr int64_t LBVH_MAX_GROUP_POINTS = (int64_t)1 << 29;
 // [first, last] (each node's index is an end of its own range), so the node is
 // local when nbase + first and nbase + last fall into one block; the flag goes
 // into its children's parent links.
-__global__ void bvh_build_kernel(Bvh b, const unsigned long long *sorted_keys)
+__global__ void bvh_build_kernel(Bvh b, const unsigned int *sorted_keys)
 {
     int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t total_nodes = b.total - b.m;
@@ -208,7 +229,7 @@ __global__ void bvh_build_kernel(Bvh b, const unsigned long long *sorted_keys)
     const int64_t nbase = b.cstart[s] - s;
     const int n = (int)b.ccount[s];
     const int i = (int)(g - nbase);
-    const unsigned long long *codes = sorted_keys + b.cstart[s];
+    const unsigned int *codes = sorted_keys + b.cstart[s];
 
     int d = karras_delta(codes, n, i, i + 1) - karras_delta(codes, n, i, i - 1) > 0 ? 1 : -1;
     if (i == 0) d = 1;
@@ -647,8 +668,8 @@ static int lbvh_group(iso_ctx *ctx, const SampleGrid &g, Segments sg, const int6
     if (total >= (int64_t)0x7fffffff) return iso_fail(ISO_ERR_CAPACITY, "too many surface points (%lld)", (long long)total);
     void *d_cstart, *d_keys, *d_keys2, *d_vals, *d_vals2, *d_compact, *d_leaves, *d_nodes, *d_pn, *d_flags, *d_misc;
     ISO_TRY(iso_buf(ctx, BUF_STAGING_A, (size_t)m * 2 * sizeof(int64_t), &d_cstart));
-    ISO_TRY(iso_buf(ctx, BUF_SORT_KEYS, (size_t)total * 8, &d_keys));
-    ISO_TRY(iso_buf(ctx, BUF_SORT_KEYS_ALT, (size_t)total * 8, &d_keys2));
+    ISO_TRY(iso_buf(ctx, BUF_SORT_KEYS, (size_t)total * 4, &d_keys));
+    ISO_TRY(iso_buf(ctx, BUF_SORT_KEYS_ALT, (size_t)total * 4, &d_keys2));
     ISO_TRY(iso_buf(ctx, BUF_SORT_VALS, (size_t)total * 4, &d_vals));
     ISO_TRY(iso_buf(ctx, BUF_SORT_VALS_ALT, (size_t)total * 4, &d_vals2));
     ISO_TRY(iso_buf(ctx, BUF_STAGING_B, (size_t)total * sizeof(float4), &d_compact));
@@ -672,7 +693,8 @@ static int lbvh_group(iso_ctx *ctx, const SampleGrid &g, Segments sg, const int6
     b.ccount = (const int64_t *)d_cstart + m;
     b.m = m;
     b.total = total;
-    b.keys = (unsigned long long *)d_keys;
+    b.keys = (unsigned int *)d_keys;
+    b.axis_bits = lbvh_axis_bits(m);
     b.vals = (unsigned int *)d_vals;
     b.compact = (float4 *)d_compact;
     b.leaves = (float4 *)d_leaves;
@@ -683,9 +705,8 @@ static int lbvh_group(iso_ctx *ctx, const SampleGrid &g, Segments sg, const int6
     const unsigned tb = (unsigned)((total + 255) / 256);
     bvh_keys_kernel<<<tb, 256, 0, ctx->stream>>>(gs, b);
     ISO_LAUNCHED(ctx);
-    int end_bit = 32;
-    while ((1ll << (end_bit - 32)) < m && end_bit < 64) ++end_bit;
-    cub::DoubleBuffer<unsigned long long> kb((unsigned long long *)d_keys, (unsigned long long *)d_keys2);
+    const int end_bit = lbvh_seg_bits(m) + 3 * b.axis_bits;
+    cub::DoubleBuffer<unsigned int> kb((unsigned int *)d_keys, (unsigned int *)d_keys2);
     cub::DoubleBuffer<unsigned int> vb((unsigned int *)d_vals, (unsigned int *)d_vals2);
     size_t temp_bytes = 0;
     ISO_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, kb, vb, (int)total, 0, end_bit, ctx->stream));
@@ -786,7 +807,8 @@ int iso_run_distance(iso_ctx *ctx, int X, int Y, int Z, int ds, int method, cons
             int64_t pts = 0;
             const int64_t cap = ctx->lbvh_group_points < LBVH_MAX_GROUP_POINTS - 1 ? ctx->lbvh_group_points
                                                                                    : LBVH_MAX_GROUP_POINTS - 1;
-            while (q1 < m && (q1 == q0 || pts + h_seg_count[q1] <= cap)) pts += h_seg_count[q1++];
+            while (q1 < m && q1 - q0 < LBVH_MAX_GROUP_SURFACES && (q1 == q0 || pts + h_seg_count[q1] <= cap))
+                pts += h_seg_count[q1++];
             ISO_TRY(lbvh_group(ctx, g, sg, h_seg_count + q0, q1 - q0, q0, fields + (size_t)q0 * field_stride,
                                field_stride));
             q0 = q1;
