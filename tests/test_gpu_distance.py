@@ -68,3 +68,26 @@ def test_reference_named_entry():
     rng = np.random.default_rng(1)
     p = rng.uniform(0, 1, (900, 3)).astype(np.float32)
     assert np.array_equal(isosim.generate_hierarchy_h(p, (16, 16, 16)), oracle.distance_field_f32(p, (16, 16, 16)))
+
+
+def test_lbvh_groups_beyond_256_surfaces(ctx):
+    """More than 256 surfaces: the LBVH is built in groups of at most 256
+    surfaces, whose sort keys carry 8 Morton bits per axis (the first group)
+    and 9 (the rest); every field equals the brute-force field bit for bit."""
+    import isosim
+    import isosim.synth as synth
+    dims = (24, 22, 20)
+    vol = synth.gaussian_blobs(dims, 5, 3, sigma=(2.0, 5.0))
+    lo, hi = float(vol.min()), float(vol.max())
+    iso = np.linspace(lo, hi, 302)[1:-1].astype(np.float32)  # 300 isovalues strictly inside
+    F = dims[0] * dims[1] * dims[2]
+    got = {}
+    for method in (isosim.DF_LBVH, isosim.DF_BRUTE):
+        _, ids, _, _ = ctx.ism(vol.ravel(), dims, iso, df_method=method, bins=64)
+        rows = np.zeros((len(ids), F), np.float32)
+        for r in range(len(ids)):
+            ctx.copy_field(r, rows[r])
+        got[method] = (ids.copy(), rows)
+    assert len(got[isosim.DF_LBVH][0]) > 256
+    assert np.array_equal(got[isosim.DF_LBVH][0], got[isosim.DF_BRUTE][0])
+    assert np.array_equal(got[isosim.DF_LBVH][1], got[isosim.DF_BRUTE][1])
