@@ -198,83 +198,15 @@ __device__ __forceinline__ void store_box(BvhNode *node, int side, float3 lo, fl
     __stcg(c + 2 + side, -hi.z);
 }
 
-// Block size of bvh_boxes_kernel, one thread per internal node.  A node whose
-// subtree's internal nodes all fall into one block of BOX_THREADS node
-// indices is "local": every arrival at it comes from that block.
+// Block size of the build and box kernels, one thread per internal node.  A
+// node whose subtree's internal nodes all fall into one block of BOX_THREADS
+// node indices is "local": every arrival at it comes from that block.  The
+// internal nodes of a subtree over leaves [first, last] have indices in
+// [first, last] (each node's index is an end of its own range), so a node is
+// local when nbase + first and nbase + last fall into one block.
 constexpr int BOX_THREADS = 256;
 // Points of one LBVH build (the parent links hold group-wide node indices * 4).
 constexpr int64_t LBVH_MAX_GROUP_POINTS = (int64_t)1 << 29;
-
-// One thread per internal node (Karras split).  Leaf children's boxes (their
-// points) are written here, and each node's arrival flag starts at its number
-// of leaf children, so the box pass starts at the nodes with two leaves.  The
-// internal nodes of a subtree over leaves [first, last] have indices in
-// [first, last] (each node's index is an end of its own range), so the node is
-// local when nbase + first and nbase + last fall into one block; the flag goes
-// into its children's parent links.
-__global__ void bvh_build_kernel(Bvh b, const unsigned int *sorted_keys)
-{
-    int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t total_nodes = b.total - b.m;
-    if (g >= total_nodes) return;
-    // segment s owns internal nodes [cstart[s] - s, cstart[s] - s + count[s] - 1)
-    int lo = 0, hi = b.m - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (b.cstart[mid] - mid <= g) lo = mid; else hi = mid - 1;
-    }
-    // one-point segments own no node and share the next segment's base; the
-    // last segment whose base is <= g owns node g
-    const int s = lo;
-    const int64_t nbase = b.cstart[s] - s;
-    const int n = (int)b.ccount[s];
-    const int i = (int)(g - nbase);
-    const unsigned int *codes = sorted_keys + b.cstart[s];
-
-    int d = karras_delta(codes, n, i, i + 1) - karras_delta(codes, n, i, i - 1) > 0 ? 1 : -1;
-    if (i == 0) d = 1;
-    int dmin = karras_delta(codes, n, i, i - d);
-    int lmax = 2;
-    while (karras_delta(codes, n, i, i + lmax * d) > dmin) lmax <<= 1;
-    int l = 0;
-    for (int t = lmax >> 1; t >= 1; t >>= 1)
-        if (karras_delta(codes, n, i, i + (l + t) * d) > dmin) l += t;
-    const int j = i + l * d;
-    const int dnode = karras_delta(codes, n, i, j);
-    int sp = 0;
-    int t = l;
-    do {
-        t = (t + 1) >> 1;
-        if (karras_delta(codes, n, i, i + (sp + t) * d) > dnode) sp += t;
-    } while (t > 1);
-    const int split = i + sp * d + (d < 0 ? -1 : 0);
-    const int first = i < j ? i : j, last = i < j ? j : i;
-    const int left = (first == split) ? (split | LEAF_BIT) : split;
-    const int right = (last == split + 1) ? ((split + 1) | LEAF_BIT) : split + 1;
-
-    BvhNode *node = b.nodes + nbase + i;
-    const bool ll = (left & LEAF_BIT) != 0, rl = (right & LEAF_BIT) != 0;
-    const float4 *lv = b.leaves + b.cstart[s];
-    if (ll && rl) {
-        const float4 p = lv[left & ~LEAF_BIT], q = lv[right & ~LEAF_BIT];
-        node->a = make_float4(p.x, q.x, p.y, q.y);
-        node->b = make_float4(p.z, q.z, -p.x, -q.x);
-        node->c = make_float4(-p.y, -q.y, -p.z, -q.z);
-    } else if (ll) {
-        const float4 p = lv[left & ~LEAF_BIT];
-        store_box(node, 0, make_float3(p.x, p.y, p.z), make_float3(p.x, p.y, p.z));
-    } else if (rl) {
-        const float4 q = lv[right & ~LEAF_BIT];
-        store_box(node, 1, make_float3(q.x, q.y, q.z), make_float3(q.x, q.y, q.z));
-    }
-    const int local = (nbase + first) / BOX_THREADS == (nbase + last) / BOX_THREADS ? 1 : 0;
-    node->d = make_int4(left, right, local, 0);
-    b.flags[nbase + i] = ((unsigned int)ll + (unsigned int)rl) | ((unsigned int)ll << 8) | ((unsigned int)rl << 9);
-    const int self = (int)(nbase + i) * 4 + local;  // group-wide index: below 2^29
-    if (!ll) b.parent_node[nbase + left] = self + 0;
-    if (!rl) b.parent_node[nbase + right] = self + 2;
-    if (i == 0) b.parent_node[nbase] = -1;
-}
 
 // Arrival count with release (this thread's box stores before it) and
 // acquire (the sibling's box stores visible after it) at device scope: one
@@ -297,88 +229,164 @@ __device__ __forceinline__ unsigned int arrive_acq_rel_cta(unsigned int *p)
     return old;
 }
 
-// Bottom-up boxes, one thread per internal node.  The climb starts at the
-// nodes with two leaf children (their boxes are complete after
-// bvh_build_kernel): a thread writes its node's box into the parent's half
-// and arrives there; the parent's flag counts leaf children plus arrivals,
-// so the thread that brings it to 2 carries on upwards with the union of its
-// box and the sibling's.
-//
-// Phase 1, local parents (every arrival from this block): the block's nodes,
-// flags and links are loaded into shared memory first (coalesced), and the
-// climb runs there, ordered by the block barrier's successor, a block-scope
-// acquire-release on the shared flag, with no global access.  The local nodes
-// whose boxes changed are then written back in one coalesced pass.  Phase 2,
-// the remaining climbs (parents whose subtrees span blocks): boxes and flags
-// in global memory, ordered at device scope.
-__global__ void __launch_bounds__(BOX_THREADS) bvh_boxes_kernel(Bvh b)
+// The box of a node from its children's halves (a, b, c as in BvhNode).
+__device__ __forceinline__ void union_of_halves(const float4 &a, const float4 &b, const float4 &c, float3 &lo,
+                                                float3 &hi)
+{
+    lo = make_float3(fminf(a.x, a.y), fminf(a.z, a.w), fminf(b.x, b.y));
+    hi = make_float3(-fminf(b.z, b.w), -fminf(c.x, c.y), -fminf(c.z, c.w));
+}
+
+// One thread per internal node: the node's Karras split, then the boxes.
+// Each node's arrival flag starts at its number of leaf children (count | left
+// leaf << 8 | right leaf << 9), so the climbs start at the nodes with two
+// leaves: a thread writes its node's box into the parent's half and arrives
+// there, and the thread that brings the flag to 2 carries on upwards with the
+// union of both halves.  The block builds its nodes into shared memory; once
+// all are built, the climbs through local parents run there (block-scope
+// acquire-release on the shared flag, no global access), and the block writes
+// every node once.  The climbs through parents that span blocks are left to
+// bvh_boxes_kernel.
+__global__ void __launch_bounds__(BOX_THREADS) bvh_build_kernel(Bvh b, const unsigned int *sorted_keys)
 {
     __shared__ unsigned int s_flag[BOX_THREADS];
-    __shared__ int s_link[BOX_THREADS];
+    __shared__ int s_link[BOX_THREADS];        // link to a local parent; -1 at a root, -2 otherwise
     __shared__ float4 s_node[BOX_THREADS][3];  // a, b, c of the block's nodes
     const int64_t total_nodes = b.total - b.m;
     const int64_t base = (int64_t)blockIdx.x * BOX_THREADS;
     const int64_t g = base + threadIdx.x;
-    int4 cd = make_int4(0, 0, 0, 0);
+    s_link[threadIdx.x] = -2;
+    __syncthreads();
+    bool climbing = false;
     if (g < total_nodes) {
-        s_flag[threadIdx.x] = b.flags[g];
-        s_link[threadIdx.x] = b.parent_node[g];
-        s_node[threadIdx.x][0] = __ldcg(&b.nodes[g].a);
-        s_node[threadIdx.x][1] = __ldcg(&b.nodes[g].b);
-        s_node[threadIdx.x][2] = __ldcg(&b.nodes[g].c);
-        cd = b.nodes[g].d;
+        // segment s owns internal nodes [cstart[s] - s, cstart[s] - s + count[s] - 1)
+        int lo = 0, hi = b.m - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (b.cstart[mid] - mid <= g) lo = mid; else hi = mid - 1;
+        }
+        // one-point segments own no node and share the next segment's base; the
+        // last segment whose base is <= g owns node g
+        const int s = lo;
+        const int64_t nbase = b.cstart[s] - s;
+        const int n = (int)b.ccount[s];
+        const int i = (int)(g - nbase);
+        const unsigned int *codes = sorted_keys + b.cstart[s];
+
+        int d = karras_delta(codes, n, i, i + 1) - karras_delta(codes, n, i, i - 1) > 0 ? 1 : -1;
+        if (i == 0) d = 1;
+        int dmin = karras_delta(codes, n, i, i - d);
+        int lmax = 2;
+        while (karras_delta(codes, n, i, i + lmax * d) > dmin) lmax <<= 1;
+        int l = 0;
+        for (int t = lmax >> 1; t >= 1; t >>= 1)
+            if (karras_delta(codes, n, i, i + (l + t) * d) > dmin) l += t;
+        const int j = i + l * d;
+        const int dnode = karras_delta(codes, n, i, j);
+        int sp = 0;
+        int t = l;
+        do {
+            t = (t + 1) >> 1;
+            if (karras_delta(codes, n, i, i + (sp + t) * d) > dnode) sp += t;
+        } while (t > 1);
+        const int split = i + sp * d + (d < 0 ? -1 : 0);
+        const int first = i < j ? i : j, last = i < j ? j : i;
+        const int left = (first == split) ? (split | LEAF_BIT) : split;
+        const int right = (last == split + 1) ? ((split + 1) | LEAF_BIT) : split + 1;
+        const bool ll = (left & LEAF_BIT) != 0, rl = (right & LEAF_BIT) != 0;
+
+        // leaf children's boxes (their points); an internal child's half is
+        // written when that child's box is complete
+        const float4 *lv = b.leaves + b.cstart[s];
+        float *half = &s_node[threadIdx.x][0].x;
+        if (ll) {
+            const float4 p = lv[left & ~LEAF_BIT];
+            half[0] = p.x, half[2] = p.y, half[4] = p.z, half[6] = -p.x, half[8] = -p.y, half[10] = -p.z;
+        }
+        if (rl) {
+            const float4 q = lv[right & ~LEAF_BIT];
+            half[1] = q.x, half[3] = q.y, half[5] = q.z, half[7] = -q.x, half[9] = -q.y, half[11] = -q.z;
+        }
+        const int local = (nbase + first) / BOX_THREADS == (nbase + last) / BOX_THREADS ? 1 : 0;
+        b.nodes[g].d = make_int4(left, right, local, 0);
+        const unsigned int flag = ((unsigned int)ll + (unsigned int)rl) | ((unsigned int)ll << 8) | ((unsigned int)rl << 9);
+        s_flag[threadIdx.x] = flag;
+        b.flags[g] = flag;
+        const int self = (int)g * 4 + local;  // group-wide index: below 2^29
+        // a local node's children are inside the block; a child index outside
+        // it would be a build error and is reported, not stored
+        auto link_child = [&](int child, int side) {
+            b.parent_node[nbase + child] = self + 2 * side;
+            if (!local) return;
+            const int64_t ct = nbase + child - base;
+            if (ct >= 0 && ct < BOX_THREADS) s_link[ct] = self + 2 * side;
+            else atomicExch(b.error, 1);
+        };
+        if (!ll) link_child(left, 0);
+        if (!rl) link_child(right, 1);
+        if (i == 0) {
+            b.parent_node[g] = -1;
+            s_link[threadIdx.x] = -1;
+        }
+        climbing = ll && rl && local;
     }
     __syncthreads();
-    bool climbing = g < total_nodes && (cd.x & LEAF_BIT) && (cd.y & LEAF_BIT);
     float3 lo = make_float3(0.f, 0.f, 0.f), hi = lo;
-    int link = -1;
+    int link = -2;
     if (climbing) {
-        const float4 ga = s_node[threadIdx.x][0], gb = s_node[threadIdx.x][1], gc = s_node[threadIdx.x][2];
-        lo = make_float3(fminf(ga.x, ga.y), fminf(ga.z, ga.w), fminf(gb.x, gb.y));
-        hi = make_float3(-fminf(gb.z, gb.w), -fminf(gc.x, gc.y), -fminf(gc.z, gc.w));
+        union_of_halves(s_node[threadIdx.x][0], s_node[threadIdx.x][1], s_node[threadIdx.x][2], lo, hi);
         link = s_link[threadIdx.x];
     }
-    // depth is bounded by the 62-bit augmented key, the loops by the node count
-    int guard = 0;
-    for (; climbing && link >= 0 && (link & 1) && guard < 4096; ++guard) {
+    // depth is bounded by the 62-bit augmented key, the loop by the node count
+    for (int guard = 0; climbing && link >= 0 && guard < 4096; ++guard) {
         const int t = (link >> 2) - (int)base, side = (link >> 1) & 1;  // parent inside this block
         if ((unsigned int)t >= (unsigned int)BOX_THREADS) {  // a local parent outside the block: a build error
             atomicExch(b.error, 1);
-            climbing = false;
             break;
         }
         float *half = &s_node[t][0].x;
         half[side] = lo.x, half[2 + side] = lo.y, half[4 + side] = lo.z;
         half[6 + side] = -hi.x, half[8 + side] = -hi.y, half[10 + side] = -hi.z;
-        if ((arrive_acq_rel_cta(&s_flag[t]) & 0xffu) == 0) {
-            climbing = false;  // sibling not done yet
-            break;
-        }
-        const float4 na = s_node[t][0], nb = s_node[t][1], nc = s_node[t][2];
-        lo = make_float3(fminf(na.x, na.y), fminf(na.z, na.w), fminf(nb.x, nb.y));
-        hi = make_float3(-fminf(nb.z, nb.w), -fminf(nc.x, nc.y), -fminf(nc.z, nc.w));
+        if ((arrive_acq_rel_cta(&s_flag[t]) & 0xffu) == 0) break;  // sibling not done yet
+        union_of_halves(s_node[t][0], s_node[t][1], s_node[t][2], lo, hi);
         link = s_link[t];
     }
     __syncthreads();
-    // write back the local nodes with an internal child (the others are
-    // unchanged, and a spanning node's halves live in global memory)
-    if (g < total_nodes && cd.z && !((cd.x & LEAF_BIT) && (cd.y & LEAF_BIT))) {
+    if (g < total_nodes) {  // every node once; spanning nodes' internal halves follow in bvh_boxes_kernel
         __stcg(&b.nodes[g].a, s_node[threadIdx.x][0]);
         __stcg(&b.nodes[g].b, s_node[threadIdx.x][1]);
         __stcg(&b.nodes[g].c, s_node[threadIdx.x][2]);
     }
-    for (; climbing && link >= 0 && guard < 4096; ++guard) {
+}
+
+// The climbs through parents that span blocks, one thread per internal node:
+// they start at the local nodes whose parent spans blocks (their boxes are
+// complete after bvh_build_kernel) and at the spanning nodes with two leaf
+// children, and go through the nodes' flags and halves in global memory,
+// ordered at device scope.  Every ancestor of a spanning node spans blocks too.
+__global__ void __launch_bounds__(BOX_THREADS) bvh_boxes_kernel(Bvh b)
+{
+    const int64_t g = (int64_t)blockIdx.x * BOX_THREADS + threadIdx.x;
+    if (g >= b.total - b.m) return;
+    const int4 cd = b.nodes[g].d;
+    int link = b.parent_node[g];
+    const bool two_leaves = (cd.x & LEAF_BIT) && (cd.y & LEAF_BIT);
+    if (!(cd.z ? (link >= 0 && !(link & 1)) : two_leaves)) return;
+    float3 lo, hi;
+    union_of_halves(__ldcg(&b.nodes[g].a), __ldcg(&b.nodes[g].b), __ldcg(&b.nodes[g].c), lo, hi);
+    for (int guard = 0; guard < 4096 && link >= 0; ++guard) {
         const int64_t pg = link >> 2;
         const int side = (link >> 1) & 1;
         BvhNode *node = b.nodes + pg;
         store_box(node, side, lo, hi);
         if ((arrive_acq_rel(&b.flags[pg]) & 0xffu) == 0) return;  // sibling not done yet
-        const float4 na = __ldcg(&node->a), nb = __ldcg(&node->b), nc = __ldcg(&node->c);
-        lo = make_float3(fminf(na.x, na.y), fminf(na.z, na.w), fminf(nb.x, nb.y));
-        hi = make_float3(-fminf(nb.z, nb.w), -fminf(nc.x, nc.y), -fminf(nc.z, nc.w));
+        float3 plo, phi;
+        union_of_halves(__ldcg(&node->a), __ldcg(&node->b), __ldcg(&node->c), plo, phi);
+        lo = plo;
+        hi = phi;
         link = b.parent_node[pg];
     }
-    if (climbing && link >= 0) atomicExch(b.error, 1);
+    if (link >= 0) atomicExch(b.error, 1);
 }
 
 __device__ __forceinline__ float max3f(float a, float b, float c)
@@ -718,7 +726,8 @@ static int lbvh_group(iso_ctx *ctx, const SampleGrid &g, Segments sg, const int6
     ISO_LAUNCHED(ctx);
     const int64_t total_nodes = total - m;
     if (total_nodes > 0) {
-        bvh_build_kernel<<<(unsigned)((total_nodes + 255) / 256), 256, 0, ctx->stream>>>(b, kb.Current());
+        bvh_build_kernel<<<(unsigned)((total_nodes + BOX_THREADS - 1) / BOX_THREADS), BOX_THREADS, 0, ctx->stream>>>(
+            b, kb.Current());
         ISO_LAUNCHED(ctx);
         bvh_boxes_kernel<<<(unsigned)((total_nodes + BOX_THREADS - 1) / BOX_THREADS), BOX_THREADS, 0, ctx->stream>>>(b);
         ISO_LAUNCHED(ctx);
