@@ -76,8 +76,9 @@ void iso_ctx_release_except_surfaces(iso_ctx *ctx)
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     for (int b = 0; b < BUF_COUNT_; ++b) {
-        if (b == BUF_VOLUME || b == BUF_ISO_SORTED || b == BUF_SURF_COUNTS || b == BUF_SURF_CURSOR ||
-            b == BUF_SEG_OFFSET || b == BUF_SEG_COUNT || b == BUF_SURF_BLOCK_COUNTS)
+        // everything the surface stage's write pass reads (iso_surface.cu)
+        if (b == BUF_VOLUME || b == BUF_ISO_SORTED || b == BUF_ISO_INDEX || b == BUF_SURF_COUNTS ||
+            b == BUF_SURF_CURSOR || b == BUF_SEG_OFFSET || b == BUF_SEG_COUNT || b == BUF_SURF_BLOCK_COUNTS)
             continue;
         if (ctx->buf[b]) cudaFree(ctx->buf[b]);
         ctx->buf[b] = nullptr;

@@ -93,6 +93,7 @@ enum IsoBuf {
     BUF_TC_OPERANDS,        // tensor-core distance: every surface's points as MMA operand rows
     BUF_REF32_SUMS,         // reference FP32 MI: column and row sums of every ordered pair
     BUF_LOGF_TABLE,         // reference FP32 MI: logf of every count below 65536
+    BUF_ISO_INDEX,          // marching cubes: bucket edges and first sorted isovalue at or above each
     BUF_COUNT_
 };
 
