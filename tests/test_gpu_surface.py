@@ -34,6 +34,22 @@ def test_mc_blobs(ctx, frame):
 
 
 @pytest.mark.parametrize("frame", [0, 1])
+def test_mc_many_clustered_isovalues(ctx, frame):
+    """80 isovalues in no order, with ten equal ones and forty within 1e-4 of
+    the range (many in one bucket of the searches' index), and the extremes
+    of the range: vertex sets and counts exact."""
+    dims = (20, 18, 16)
+    vol = blobs(dims, 7)
+    lo, hi = float(vol.min()), float(vol.max())
+    rng = np.random.default_rng(11)
+    c = lo + 0.3 * (hi - lo)
+    isos = np.concatenate([rng.uniform(lo, hi, 28), [lo, hi], c + rng.uniform(0, 1e-4 * (hi - lo), 40),
+                           np.full(10, c)]).astype(np.float32)
+    rng.shuffle(isos)
+    check_mc(ctx, vol, dims, isos, frame)
+
+
+@pytest.mark.parametrize("frame", [0, 1])
 def test_mc_noncubic_noise(ctx, frame):
     dims = (17, 13, 9)
     vol = np.random.default_rng(4).standard_normal(dims).astype(np.float32)
