@@ -465,7 +465,7 @@ __device__ __forceinline__ void traverse_packet(const BvhNode *nodes, const Quer
                                                 float3 (&bp)[K], int *error)
 {
     int stack[STACK_DEPTH];      // warp-uniform node ids
-    float sd[K][STACK_DEPTH];    // each sample's distance to each postponed node
+    float sd[STACK_DEPTH];       // the lane's nearest sample distance to each postponed node
     int top = 0;
     int cur = 0;
     for (;;) {
@@ -509,7 +509,10 @@ __device__ __forceinline__ void traverse_packet(const BvhNode *nodes, const Quer
             }
             stack[top] = lfirst ? right : left;
 #pragma unroll
-            for (int k = 0; k < K; ++k) sd[k][top] = lfirst ? dd[k].y : dd[k].x;
+            float near = lfirst ? dd[0].y : dd[0].x;
+#pragma unroll
+            for (int k = 1; k < K; ++k) near = fminf(near, lfirst ? dd[k].y : dd[k].x);
+            sd[top] = near;
             ++top;
             cur = lfirst ? left : right;
         } else if (any_l) {
@@ -519,9 +522,10 @@ __device__ __forceinline__ void traverse_packet(const BvhNode *nodes, const Quer
         } else {
             for (;;) {
                 if (top == 0) break;
-                bool keep = false;
+                float loosest = best[0];
 #pragma unroll
-                for (int k = 0; k < K; ++k) keep |= sd[k][top - 1] < best[k];
+                for (int k = 1; k < K; ++k) loosest = fmaxf(loosest, best[k]);
+                const bool keep = sd[top - 1] < loosest;  // skipped only where no sample's bound admits it
                 if (__any_sync(0xffffffffu, keep)) break;
                 --top;
             }
